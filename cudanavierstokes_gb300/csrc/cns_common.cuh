@@ -1,0 +1,85 @@
+// cns_common.cuh -- device-side layout, constants and helpers shared by all kernels.
+//
+// HBM layout: every field is an FP64 (or FP32, for the FP32-RHS stencil inputs) 3D
+// array with a ghost layer of width G = S (the advective half-width) on all six faces,
+// x fastest. Ghost cells hold the reference's boundary images (periodic copies,
+// wall mirrors, isothermal-wall temperature, extrapolation), filled once per stage by
+// the ghost kernels, so the stencil kernels index neighbours with plain strides and
+// no boundary branches. This replaces the reference's per-pencil shared-memory
+// ghost fills (src/boundary.h, src/boundary_condition_{x,y,z}.h) and its MPI halos.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace cns {
+
+enum XBC { XBC_PER = 0, XBC_WALL = 1, XBC_BL = 2 };
+
+// indices into the device scalar block
+enum { SC_DT = 0, SC_DPDZ = 1, SC_TIME = 2, SC_NONFINITE = 3, SC_COUNT = 8 };
+
+struct Geom {
+    int mx, my, mz, G;
+    long long P;      // row pitch (elements)
+    long long PS;     // plane stride (elements)
+    long long base;   // element offset of interior point (0,0,0)
+    int xbc;          // XBC_*
+    int zbl;          // 1: z ends extrapolated (boundary layer), 0: periodic
+    int nonuniform_x;
+    const double* xp;     // [mx] 1/x'(xi)
+    const double* cvsx;   // [(2V+1)*mx] non-uniform x second-derivative weights, index it*mx+i
+    const double* wvol;   // [mx] cell volume dxv[i]/d_dy/d_dz
+    const double* dxv;    // [mx] cell widths
+    double dx, dy, dz, d2x, d2y, d2z;   // inverse spacings and their squares
+
+    __host__ __device__ __forceinline__ long long at(int i, int j, int k) const {
+        return base + (long long)k * PS + (long long)j * P + i;
+    }
+};
+
+struct Phys {
+    double gam, Rgas, Re, Pr, Ec, vexp;
+    double invRe, clam, cvInv, hcoef;   // 1/Re, 1/(Re Pr Ec), (gam-1)/Rgas, Rgas*gam/(gam-1)
+    double twall_top, twall_bot, cfl, Lx, Ly, Lz;
+    int vexp_is_one, quirk, perturbed;
+    int pert_kc, pert_lp;
+    double pert_amp1, pert_amp2, pert_omega1, pert_omega2, pert_lambda;
+};
+
+// Stencil coefficients premultiplied by the inverse grid spacing of each direction,
+// in the arithmetic type R of the kernel that uses them.
+//   c1S[d][k]: first derivative at the advective order 2S,  D f = sum_k c1S[k] (f_{+k} - f_{-k})
+//   c1V[d][k]: first derivative at the viscous order 2V
+//   c2V[d][k]: second derivative at order 2V (uniform), D2 f = c2V[0] f_0 + sum_k c2V[k](f_{+k}+f_{-k})
+// from the central tables of src/globals.h:69-95 (c1[k] = -coeffF[K-k], c2[k] = coeffS[K-k]).
+// xp / cvsx are the non-uniform x metric tables in type R.
+template <typename R>
+struct CoefT {
+    R c1S[3][5];
+    R c1V[3][5];
+    R c2V[3][5];
+    const R* xp;     // [mx]
+    const R* cvsx;   // [(2V+1)*mx], index it*mx + i
+};
+
+// perturbation of the bottom-wall u ghosts (src/perturbation.h:25-53)
+__device__ __forceinline__ bool wall_perturbation(const Phys& ph, double dy_inv, int j, int k, double time,
+                                                  double* val) {
+    int kSt = ph.pert_kc - ph.pert_lp / 2, kEn = ph.pert_kc + ph.pert_lp / 2;
+    if (k < kSt || k > kEn) return false;
+    int alpha, beta, kappa;
+    if (k < ph.pert_kc) { kappa = 1; alpha = k - kSt; beta = ph.pert_kc - kSt; }
+    else { kappa = -1; alpha = kEn - k; beta = kEn - ph.pert_kc; }
+    double ksi = alpha * 1.0 / beta;
+    double g = (15.1875 * ksi * ksi * ksi * ksi * ksi) - (35.4375 * ksi * ksi * ksi * ksi) + (20.25 * ksi * ksi * ksi);
+    double y_glob = j / dy_inv;
+    *val = ph.pert_amp1 * kappa * g * sin(ph.pert_omega1 * time) +
+           ph.pert_amp2 * kappa * g * sin(ph.pert_omega2 * time) * cos(y_glob / ph.pert_lambda);
+    return true;
+}
+
+template <typename R> __device__ __forceinline__ R cns_pow(R a, R b);
+template <> __device__ __forceinline__ double cns_pow<double>(double a, double b) { return pow(a, b); }
+template <> __device__ __forceinline__ float cns_pow<float>(float a, float b) { return powf(a, b); }
+
+}  // namespace cns

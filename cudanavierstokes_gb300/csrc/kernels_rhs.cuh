@@ -1,0 +1,228 @@
+// kernels_rhs.cuh -- the RHS + Runge-Kutta stage kernel (one thread per grid point).
+//
+// Per point it forms the x, y and z contributions of deviceRHSX/Y/Z
+// (src/cuda_rhs.cu:9-396), the body force, the sponge (src/sponge.cu:31-41) and then
+// the stage update of the selected time scheme (sumLowStorageRK3 + deviceMul/deviceDiv,
+// src/cuda_main.cu:109-186,244-247; eulerSum*/rk3final*, src/cuda_main.cu:188-216),
+// writing the new state to the other state buffer. All neighbour reads hit the ghosted
+// layout, so there is no boundary branching.
+//
+// The split-form convective derivative is evaluated in its telescoped form. The
+// reference accumulates the two interface fluxes F_{i+1/2}, F_{i-1/2} over every
+// (l, m) pair of the Kennedy-Gruber sum (src/cuda_derivs.h:30-155) and differences
+// them; all pairs except (i-l, i) and (i, i+l) cancel exactly, so
+//   d(f g h)/dx |_i = c/dx * sum_l a_l [ P(i-l, i) - P(i, i+l) ],
+//   P(a, b) = (f_a + f_b)(g_a + g_b)(h_a + h_b),  a_l = -coeffF[S-l],  c = 1/2 (two
+//   factors) or 1/4 (three factors),
+// which is the same value with 2 instead of l(l+1) pair products per l. The product
+// (rho_a+rho_b)(g_a+g_b) is shared by the mass flux and the four cubic fluxes.
+#pragma once
+#include "cns_common.cuh"
+#include "cns_internal.h"
+
+namespace cns {
+
+template <typename R>
+__device__ __forceinline__ R ld(const R* __restrict__ p, long long o) { return __ldg(p + o); }
+
+template <typename R, int K>
+__device__ __forceinline__ R d1(const R* __restrict__ f, long long c, long long st, const R* co) {
+    R s = co[1] * (ld(f, c + st) - ld(f, c - st));
+#pragma unroll
+    for (int k = 2; k <= K; k++) s = fma(co[k], ld(f, c + k * st) - ld(f, c - k * st), s);
+    return s;
+}
+
+template <typename R, int K>
+__device__ __forceinline__ R d2u(const R* __restrict__ f, long long c, long long st, const R* co) {
+    R s = co[0] * ld(f, c);
+#pragma unroll
+    for (int k = 1; k <= K; k++) s = fma(co[k], ld(f, c + k * st) + ld(f, c - k * st), s);
+    return s;
+}
+
+// non-uniform x second derivative with the per-point table (derDevSharedV2x, nonUniformX)
+template <typename R, int V>
+__device__ __forceinline__ R d2x_nu(const R* __restrict__ f, long long c, const R* __restrict__ cvsx, int mx, int i) {
+    R s = (R)0;
+#pragma unroll
+    for (int it = 0; it < 2 * V + 1; it++) s = fma(__ldg(cvsx + it * mx + i), ld(f, c + (it - V)), s);
+    return s;
+}
+
+template <typename R, int S, int V, int DIR>
+__device__ __forceinline__ void rhs_direction(const Geom& g, const CoefT<R>& cf, const RhsIn<R>& in, long long c,
+                                              int i, const R (&Gr)[9], R th0, R m0, R l0, R u0, R v0, R w0, R r0,
+                                              R h0, int quirk, R (&acc)[5]) {
+    const long long st = DIR == 0 ? 1LL : (DIR == 1 ? g.P : g.PS);
+    const bool nux = (DIR == 0) && g.nonuniform_x;
+    const R xpi = nux ? cf.xp[i] : (R)1;
+    const R* c1V = cf.c1V[DIR];
+    const R* c1S = cf.c1S[DIR];
+    const R* c2V = cf.c2V[DIR];
+
+    // stress row tau_{DIR, c} / mu  (uXtmp, vXtmp, wXtmp of deviceRHSX and its y/z twins)
+    R tau[3];
+#pragma unroll
+    for (int q = 0; q < 3; q++)
+        tau[q] = (q == DIR) ? (R)2 * Gr[3 * DIR + q] - (R)(2. / 3.) * th0 : Gr[3 * DIR + q] + Gr[3 * q + DIR];
+    // viscous dissipation tau_{DIR,c} d u_c / d x_DIR (y: tau_yz * dv/dz with the quirk, cuda_rhs.cu:175)
+    const R dw = (DIR == 1 && quirk) ? Gr[7] : Gr[3 * DIR + 2];
+    R e = m0 * (tau[0] * Gr[3 * DIR + 0] + tau[1] * Gr[3 * DIR + 1] + tau[2] * dw);
+
+    const R dmu = d1<R, V>(in.m, c, st, c1V) * xpi;
+    tau[0] *= dmu; tau[1] *= dmu; tau[2] *= dmu;
+    R d2uu, d2vv, d2ww, d2tt;
+    if (nux) {
+        d2uu = d2x_nu<R, V>(in.u, c, cf.cvsx, g.mx, i);
+        d2vv = d2x_nu<R, V>(in.v, c, cf.cvsx, g.mx, i);
+        d2ww = d2x_nu<R, V>(in.w, c, cf.cvsx, g.mx, i);
+        d2tt = d2x_nu<R, V>(in.t, c, cf.cvsx, g.mx, i);
+    } else {
+        d2uu = d2u<R, V>(in.u, c, st, c2V);
+        d2vv = d2u<R, V>(in.v, c, st, c2V);
+        d2ww = d2u<R, V>(in.w, c, st, c2V);
+        d2tt = d2u<R, V>(in.t, c, st, c2V);
+    }
+    tau[0] = fma(d2uu, m0, tau[0]);
+    tau[1] = fma(d2vv, m0, tau[1]);
+    tau[2] = fma(d2ww, m0, tau[2]);
+    e = e + u0 * tau[0] + v0 * tau[1] + w0 * tau[2];
+    // heat conduction: lambda d2T + dlambda dT
+    e = fma(d2tt, l0, e);
+    const R dl = d1<R, V>(in.l, c, st, c1V) * xpi;
+    const R dt = d1<R, V>(in.t, c, st, c1V) * xpi;
+    e = fma(dt, dl, e);
+    // mu/3 d(theta) and the pressure gradient on the DIR momentum
+    const R dth = d1<R, V>(in.dil, c, st, c1V) * xpi;
+    const R dp = d1<R, S>(in.p, c, st, c1S) * xpi;
+    const R mth = m0 * dth / (R)3.0;
+    const R un = DIR == 0 ? u0 : (DIR == 1 ? v0 : w0);
+    tau[DIR] = tau[DIR] + mth - dp;
+    e = fma(mth, un, e);
+
+    // split-form convective derivatives, telescoped (see file comment)
+    const R* gv = DIR == 0 ? in.u : (DIR == 1 ? in.v : in.w);
+    R fr = 0, fu = 0, fv = 0, fw = 0, fe = 0;
+#pragma unroll
+    for (int l = 1; l <= S; l++) {
+        const long long o = l * st;
+        const R rm = ld(in.r, c - o), rp = ld(in.r, c + o);
+        const R um = ld(in.u, c - o), up = ld(in.u, c + o);
+        const R vm = ld(in.v, c - o), vp = ld(in.v, c + o);
+        const R wm = ld(in.w, c - o), wp = ld(in.w, c + o);
+        const R hm = ld(in.h, c - o), hp = ld(in.h, c + o);
+        const R gm = DIR == 0 ? um : (DIR == 1 ? vm : wm);
+        const R gp = DIR == 0 ? up : (DIR == 1 ? vp : wp);
+        (void)gv;
+        const R Qm = (rm + r0) * (gm + un);
+        const R Qp = (r0 + rp) * (un + gp);
+        const R a = c1S[l];
+        fr = fma(a, Qm - Qp, fr);
+        fu = fma(a, Qm * (um + u0) - Qp * (u0 + up), fu);
+        fv = fma(a, Qm * (vm + v0) - Qp * (v0 + vp), fv);
+        fw = fma(a, Qm * (wm + w0) - Qp * (w0 + wp), fw);
+        fe = fma(a, Qm * (hm + h0) - Qp * (h0 + hp), fe);
+    }
+    const R cq = (R)0.5 * xpi, cc = (R)0.25 * xpi;
+    acc[0] = fma(cq, fr, acc[0]);
+    acc[1] = acc[1] + tau[0] + cc * fu;
+    acc[2] = acc[2] + tau[1] + cc * fv;
+    acc[3] = acc[3] + tau[2] + cc * fw;
+    acc[4] = acc[4] + e + cc * fe;
+}
+
+template <typename R, int S, int V>
+__global__ void __launch_bounds__(128) k_rhs(Geom g, CoefT<R> cf, RhsIn<R> in, Update<R> up,
+                                             const double* __restrict__ scal, int quirk) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y;
+    const int k = blockIdx.z;
+    if (i >= g.mx || j >= g.my) return;
+    const long long c = g.at(i, j, k);
+
+    R Gr[9];
+#pragma unroll
+    for (int q = 0; q < 9; q++) Gr[q] = ld(in.g[q], c);
+    const R th0 = ld(in.dil, c), m0 = ld(in.m, c), l0 = ld(in.l, c);
+    const R u0 = ld(in.u, c), v0 = ld(in.v, c), w0 = ld(in.w, c), r0 = ld(in.r, c), h0 = ld(in.h, c);
+    R acc[5] = {0, 0, 0, 0, 0};
+    rhs_direction<R, S, V, 0>(g, cf, in, c, i, Gr, th0, m0, l0, u0, v0, w0, r0, h0, quirk, acc);
+    rhs_direction<R, S, V, 1>(g, cf, in, c, i, Gr, th0, m0, l0, u0, v0, w0, r0, h0, quirk, acc);
+    rhs_direction<R, S, V, 2>(g, cf, in, c, i, Gr, th0, m0, l0, u0, v0, w0, r0, h0, quirk, acc);
+
+    // ---- FP64 from here: body force, sponge, stage update ----
+    const double dpdz = scal[SC_DPDZ];
+    const double rr = up.qin.r[c], uu = up.qin.u[c], vv = up.qin.v[c], ww = up.qin.w[c], ee = up.qin.e[c];
+    double Rd[5] = {(double)acc[0], (double)acc[1], (double)acc[2], (double)acc[3], (double)acc[4]};
+    Rd[3] += dpdz;
+    Rd[4] += dpdz * (double)w0;
+    if (up.spx) {
+        const double s = up.spx[i] + up.spz[k];
+        const long long i2 = (long long)i + (long long)k * g.mx;
+        Rd[0] += s * (up.rref[i2] - rr);
+        Rd[1] += s * (up.uref[i2] - rr * uu);
+        Rd[2] += s * (up.vref[i2] - rr * vv);
+        Rd[3] += s * (up.wref[i2] - rr * ww);
+        Rd[4] += s * (up.eref[i2] - ee);
+    }
+    if (up.kind == ST_RHS_ONLY) {
+#pragma unroll
+        for (int q = 0; q < 5; q++) up.rb[q][c] = (R)Rd[q];
+        return;
+    }
+    const double dt = scal[SC_DT];
+    double qn[5];
+    if (up.kind == ST_LS) {
+        const double q0[5] = {rr, uu * rr, vv * rr, ww * rr, ee};
+#pragma unroll
+        for (int q = 0; q < 5; q++) {
+            const double x = up.a != 0.0 ? up.a * (double)up.rb[q][c] + up.b * Rd[q] : up.b * Rd[q];
+            qn[q] = q0[q] + dt * x;
+            up.rb[q][c] = (R)Rd[q];
+        }
+    } else if (up.kind == ST_C1 || up.kind == ST_R4_1) {
+        const double q0[5] = {rr, rr * uu, rr * vv, rr * ww, ee};
+#pragma unroll
+        for (int q = 0; q < 5; q++) {
+            up.q0[q][c] = q0[q];
+            if (up.kind == ST_C1) { qn[q] = q0[q] + Rd[q] * dt / 2.0; up.rb[q][c] = (R)Rd[q]; }
+            else { qn[q] = q0[q] + 0.5 * dt * Rd[q]; up.k2[q][c] = (R)Rd[q]; }
+        }
+    } else {
+        double q0[5];
+#pragma unroll
+        for (int q = 0; q < 5; q++) q0[q] = up.q0[q][c];
+#pragma unroll
+        for (int q = 0; q < 5; q++) {
+            switch (up.kind) {
+            case ST_C2: qn[q] = q0[q] + (2 * Rd[q] - (double)up.rb[q][c]) * dt; up.k2[q][c] = (R)Rd[q]; break;
+            case ST_C3: qn[q] = q0[q] + dt * ((double)up.rb[q][c] + 4 * (double)up.k2[q][c] + Rd[q]) / 6.; break;
+            case ST_R4_2: up.k2[q][c] = (R)((double)up.k2[q][c] + 2.0 * Rd[q]); qn[q] = q0[q] + 0.5 * dt * Rd[q]; break;
+            case ST_R4_3: up.k2[q][c] = (R)((double)up.k2[q][c] + 2.0 * Rd[q]); qn[q] = q0[q] + dt * Rd[q]; break;
+            default: qn[q] = q0[q] + dt / 6.0 * ((double)up.k2[q][c] + Rd[q]); break;
+            }
+        }
+    }
+    const double inv = 1.0 / qn[0];
+    up.qout.r[c] = qn[0];
+    up.qout.u[c] = qn[1] * inv;
+    up.qout.v[c] = qn[2] * inv;
+    up.qout.w[c] = qn[3] * inv;
+    up.qout.e[c] = qn[4];
+}
+
+template <typename R>
+void launch_rhs_t(int S, int V, const Geom& g, const CoefT<R>& cf, const RhsIn<R>& in, const Update<R>& up,
+                  const double* scal, int quirk, cudaStream_t s) {
+    dim3 grid((g.mx + 31) / 32, (g.my + 3) / 4, g.mz), block(32, 4, 1);
+#define CNS_RHS_CASE(SS, VV) \
+    if (S == SS && V == VV) { k_rhs<R, SS, VV><<<grid, block, 0, s>>>(g, cf, in, up, scal, quirk); return; }
+    CNS_RHS_CASE(1, 1)
+    CNS_RHS_CASE(2, 1) CNS_RHS_CASE(2, 2)
+    CNS_RHS_CASE(3, 1) CNS_RHS_CASE(3, 2) CNS_RHS_CASE(3, 3)
+    CNS_RHS_CASE(4, 1) CNS_RHS_CASE(4, 2) CNS_RHS_CASE(4, 3) CNS_RHS_CASE(4, 4)
+#undef CNS_RHS_CASE
+}
+
+}  // namespace cns

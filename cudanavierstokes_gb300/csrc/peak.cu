@@ -1,0 +1,52 @@
+// peak.cu -- FMA-throughput probe used to state the FP64 / FP32 pipe roofline next to the
+// measured HBM bandwidth (the stencil path is bounded by the FP64 pipe, not by HBM).
+#include <cuda_runtime.h>
+
+#include "../../include/cns.h"
+
+namespace {
+
+template <typename T>
+__global__ void __launch_bounds__(256) k_fma_peak(T* out, int iters, T a, T b) {
+    T x0 = (T)threadIdx.x, x1 = x0 + (T)1, x2 = x0 + (T)2, x3 = x0 + (T)3;
+    T x4 = x0 + (T)4, x5 = x0 + (T)5, x6 = x0 + (T)6, x7 = x0 + (T)7;
+    for (int it = 0; it < iters; it++) {
+        x0 = fma(x0, a, b); x1 = fma(x1, a, b); x2 = fma(x2, a, b); x3 = fma(x3, a, b);
+        x4 = fma(x4, a, b); x5 = fma(x5, a, b); x6 = fma(x6, a, b); x7 = fma(x7, a, b);
+    }
+    T s = ((x0 + x1) + (x2 + x3)) + ((x4 + x5) + (x6 + x7));
+    if (s == (T)-12345.0) out[blockIdx.x] = s;   // never true; keeps the chains live
+}
+
+template <typename T>
+int probe(int device, int iters, double* tflops) {
+    if (cudaSetDevice(device) != cudaSuccess) return CNS_ERR_CUDA;
+    int nsm = 0;
+    cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, device);
+    const int blocks = nsm * 8, threads = 256;
+    T* out = nullptr;
+    if (cudaMalloc(&out, blocks * sizeof(T)) != cudaSuccess) return CNS_ERR_OOM;
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    k_fma_peak<T><<<blocks, threads>>>(out, iters / 10, (T)0.999999, (T)1e-7);   // warm-up
+    cudaEventRecord(e0);
+    k_fma_peak<T><<<blocks, threads>>>(out, iters, (T)0.999999, (T)1e-7);
+    cudaEventRecord(e1);
+    cudaError_t err = cudaEventSynchronize(e1);
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, e0, e1);
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    cudaFree(out);
+    if (err != cudaSuccess) return CNS_ERR_CUDA;
+    *tflops = 2.0 * 8.0 * (double)blocks * threads * (double)iters / (ms * 1e-3) / 1e12;
+    return CNS_OK;
+}
+
+}  // namespace
+
+extern "C" int cns_probe_fma_peak(int device, int fp64, int iters, double* tflops) {
+    if (!tflops || iters < 10) return CNS_ERR_INVALID;
+    return fp64 ? probe<double>(device, iters, tflops) : probe<float>(device, iters, tflops);
+}

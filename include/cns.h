@@ -1,0 +1,200 @@
+/*
+ * cns.h -- C ABI of the GB300 (sm_103a) time-advance path for the 3D compressible
+ * Navier-Stokes equations (conservative split-form RHS + Runge-Kutta stage update).
+ *
+ * This header is the drop-in boundary for the host-side call sequence of
+ * CudaNavierStokes (src/main.h:23-42, src/cuda_main.cu:109-186,249-265):
+ *
+ *   reference                                      this ABI
+ *   ---------------------------------------------  -------------------------------------
+ *   compile-time macros  src/globals.h:5-95        cns_params (runtime), cns_default_params
+ *   setDevice + setGPUParameters + initSolver      cns_create
+ *       (src/cuda_utils.cu:49-179,415-519,816)
+ *   initGrid / derivGrid (src/init.cpp:32-92,258)  cns_get_grid (grid built inside cns_create)
+ *   calculateSponge (src/sponge.cu:83-240)         cns_set_sponge_profiles / cns_set_sponge
+ *   copyField(0) / copyField(1)                    cns_copy_field
+ *       (src/cuda_utils.cu:299-370)
+ *   runSimulationLowStorage / runSimulation        cns_run
+ *       (src/cuda_main.cu:109-186, :44-107)
+ *   calcRHS (src/cuda_main.cu:15-42)               cns_calc_rhs   (test hook)
+ *   calcTimeStepPressGrad (src/cuda_main.cu:249)   cns_get_scalars (dt, dpdz, time)
+ *   clearSolver (src/cuda_utils.cu:521-595)        cns_destroy
+ *
+ * Conventions
+ *   - All fields are FP64, x fastest: index(i,j,k) = i + j*mx + k*mx*my
+ *     (src/globals.h:60-61). The stored state is rho, primitive u, v, w and rho*E,
+ *     exactly as the reference's d_r, d_u, d_v, d_w, d_e (src/cuda_main.h:14-18).
+ *   - Host arrays are caller-owned; the library copies in and out. Device state is
+ *     owned by the handle.
+ *   - Every call returns an int status (CNS_OK = 0). cns_last_error() gives a
+ *     thread-local message for the last failure on the calling thread.
+ *   - A handle is used from one host thread at a time. Work is issued on the
+ *     handle's stream (cns_set_stream); calls that return host data synchronise it.
+ *   - The product path has no CPU fallback: without a usable CUDA device every
+ *     entry point that needs one returns CNS_ERR_CUDA.
+ */
+#ifndef CNS_GB300_H_
+#define CNS_GB300_H_
+
+#include <stddef.h>
+#include <stdint.h>
+
+#if defined(__GNUC__)
+#define CNS_API __attribute__((visibility("default")))
+#else
+#define CNS_API
+#endif
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* status codes */
+#define CNS_OK             0
+#define CNS_ERR_INVALID    1   /* bad parameter or argument                         */
+#define CNS_ERR_CUDA       2   /* CUDA runtime error / no device                     */
+#define CNS_ERR_OOM        3   /* device allocation failed or HBM budget exceeded    */
+#define CNS_ERR_NONFINITE  4   /* non-finite or non-physical state detected          */
+#define CNS_ERR_TIMEOUT    5   /* a bounded device wait gave up                      */
+#define CNS_ERR_STATE      6   /* call made in the wrong order (e.g. run before init) */
+
+/* time schemes */
+#define CNS_RK3_LOWSTORAGE 0   /* Wray low-storage RK3 (src/cuda_main.cu:10-11,109-186) */
+#define CNS_RK3_CLASSIC    1   /* classic 3-stage RK3  (src/cuda_main.cu:44-107,188-216) */
+#define CNS_RK4_CLASSIC    2   /* classic 4-stage RK4: no counterpart in the reference   */
+
+/* RHS arithmetic */
+#define CNS_PREC_FP64      0   /* plain FP64 everywhere, as the reference                */
+#define CNS_PREC_FP32_RHS  1   /* RHS in FP32; state, RK accumulation, T/p recovery and
+                                  reductions in FP64                                     */
+
+/*
+ * Runtime mirror of the reference's compile-time parameter surface
+ * (src/globals.h:14-58, src/sponge.h:4-17, src/perturbation.h:14-22).
+ * Axis convention is the reference's: x is the only non-periodic / stretched /
+ * wall-normal direction, y is periodic, z is periodic or (boundary layer)
+ * extrapolated; the channel body force acts on z momentum.
+ */
+typedef struct cns_params {
+    int32_t mx, my, mz;          /* mx_tot, my_tot, mz_tot (globals.h:24-26)            */
+    double  Lx, Ly, Lz;          /* domain lengths (globals.h:21-23)                     */
+    int32_t stencil_size;        /* S: advective half-width, order 2S, 1..4 (globals.h:18) */
+    int32_t stencil_visc;        /* V: viscous half-width, order 2V, 1..S (globals.h:19)   */
+    double  Re, Pr, Ma, gam, viscexp;   /* globals.h:42-46                               */
+    double  cfl;                 /* CFL (globals.h:29)                                   */
+    int32_t scheme;              /* CNS_RK3_LOWSTORAGE (lowStorage=true) or CNS_RK3_CLASSIC */
+    int32_t boundary_layer;      /* boundaryLayer (globals.h:33)                          */
+    int32_t perturbed;           /* perturbed (globals.h:34)                              */
+    int32_t forcing;             /* forcing: constant-mass-flux body force on z (globals.h:35) */
+    int32_t periodic_x;          /* periodicX (globals.h:36)                              */
+    int32_t nonuniform_x;        /* nonUniformX: tanh-stretched x (globals.h:37)          */
+    double  stretch;             /* tanh stretching factor (globals.h:50)                 */
+    double  twall_top, twall_bot;/* isothermal wall temperatures (globals.h:51-52)        */
+    int32_t check_cfl;           /* checkCFLcondition: dt (and forcing) update period     */
+    int32_t check_bulk;          /* checkBulk: bulk / kinetic-energy diagnostic period    */
+    int32_t quirk_dissipation_y; /* 1: reproduce the reference's y viscous-dissipation
+                                    term tau_yz*dv/dz (src/cuda_rhs.cu:175); 0: tau_yz*dw/dy */
+    int32_t precision;           /* CNS_PREC_FP64 or CNS_PREC_FP32_RHS                     */
+    int32_t ndivz;               /* nDivZ (globals.h:58): accepted for compatibility, no effect */
+    double  dpdz_init;           /* initial body force when forcing (cuda_utils.cu:69: 0.00372) */
+    /* sponge constants (src/sponge.h:4-17) */
+    double  sp_top_str, sp_top_len, sp_top_exp;
+    double  sp_inl_str, sp_inl_len, sp_inl_exp;
+    double  sp_out_str, sp_out_len, sp_out_exp;
+    /* wall perturbation constants (src/perturbation.h:14-22) */
+    int32_t pert_kc, pert_lp;
+    double  pert_amp1, pert_amp2, pert_omega1_per_re, pert_omega2;
+} cns_params;
+
+typedef struct cns_solver cns_solver;
+
+/* Fill *p with the values of the reference's src/globals.h / sponge.h / perturbation.h
+ * defaults for everything that is not a grid size (grid set to 64^3 periodic TGV). */
+CNS_API void        cns_default_params(cns_params* p);
+
+/* Validate parameters without touching a device. Returns CNS_OK or CNS_ERR_INVALID. */
+CNS_API int         cns_check_params(const cns_params* p);
+
+/* Thread-local message describing the last failure on this thread ("" if none). */
+CNS_API const char* cns_last_error(void);
+
+/* Library version string. */
+CNS_API const char* cns_version(void);
+
+/* setDevice + setGPUParameters + initSolver (src/cuda_utils.cu:49-179,415-519):
+ * builds the grid (src/init.cpp:32-92), coefficient tables and allocates the
+ * device state on `device`. */
+CNS_API int cns_create(const cns_params* p, int device, cns_solver** out);
+
+/* clearSolver (src/cuda_utils.cu:521-595). NULL is accepted. */
+CNS_API int cns_destroy(cns_solver* h);
+
+/* Set the CUDA stream (a cudaStream_t cast to void*) for all work of this handle.
+ * NULL selects the handle's own stream. */
+CNS_API int cns_set_stream(cns_solver* h, void* stream);
+
+/* Grid built by initGrid/derivGrid (src/init.cpp:32-92,258-277): x[mx], xp[mx]
+ * (= 1/x'(xi)), xpp[mx] (= x''(xi)), y[my], z[mz]. Any pointer may be NULL. */
+CNS_API int cns_get_grid(cns_solver* h, double* x, double* xp, double* xpp, double* y, double* z);
+
+/* calculateSponge (src/sponge.cu:83-240) from a 1D self-similar profile
+ * (the reference's blasius1D/{x,r,u,w,e}Prof.bin): sponge strengths from the sponge
+ * constants, reference fields by cubic-spline interpolation of the profile at
+ * x/sqrt(1+z/Re). When `init_fields` is non-zero the state is also set to the
+ * reference fields (restartFile < 0 in the reference). */
+CNS_API int cns_set_sponge_profiles(cns_solver* h, int n, const double* xin, const double* rin,
+                            const double* uin, const double* win, const double* ein,
+                            int init_fields);
+
+/* Direct form: sponge_x[mx], sponge_z[mz] and the reference fields r, u, w, rhoE
+ * on the (x,z) plane, each mx*mz, index i + k*mx (src/sponge.h:36-37). u_ref and
+ * w_ref are velocities; momentum references are formed as in copySpongeToDevice
+ * (src/sponge.cu:57-61). */
+CNS_API int cns_set_sponge(cns_solver* h, const double* sponge_x, const double* sponge_z,
+                   const double* rref, const double* uref, const double* wref,
+                   const double* eref);
+
+/* copyField (src/cuda_utils.cu:299-370). direction 0: host -> device, followed by
+ * the state recomputation (calcState). direction 1: device -> host. */
+CNS_API int cns_copy_field(cns_solver* h, int direction, double* r, double* u, double* v,
+                   double* w, double* e);
+
+/* runSimulationLowStorage / runSimulation (src/cuda_main.cu:109-186, :44-107):
+ * advance `nsteps` time steps. Every check_cfl steps (counted from the handle's
+ * step counter) dt and, with forcing, the body force are recomputed on the device;
+ * every check_bulk steps the bulk diagnostic is evaluated. The optional host
+ * arrays par1, par2, time (length nsteps) receive, per step, the bulk diagnostics
+ * (kinetic energy <u.u> when not forced; bulk velocity and integral of rhoE when
+ * forced; NaN on steps without a diagnostic) and the simulation time after the
+ * step, as the reference's dpar1/dpar2/dtime. */
+CNS_API int cns_run(cns_solver* h, int nsteps, double* par1, double* par2, double* time);
+
+/* One evaluation of calcRHS (src/cuda_main.cu:15-42) on the current state, copied to
+ * the host: d(rho)/dt, d(rho u)/dt, d(rho v)/dt, d(rho w)/dt, d(rho E)/dt. */
+CNS_API int cns_calc_rhs(cns_solver* h, double* rr, double* ru, double* rv, double* rw, double* re);
+
+/* Current dt, body force dpdz and simulation time (device scalars dtC, dpdz,
+ * time_on_GPU of the reference). Any pointer may be NULL. */
+CNS_API int cns_get_scalars(cns_solver* h, double* dt, double* dpdz, double* time);
+
+/* Override dt, dpdz, simulation time and the step counter (restart bookkeeping).
+ * Negative step leaves the counter unchanged. */
+CNS_API int cns_set_scalars(cns_solver* h, double dt, double dpdz, double time, int64_t step);
+
+/* Number of CUDA kernels this handle has launched since creation. */
+CNS_API int64_t cns_kernel_launches(const cns_solver* h);
+
+/* Device bytes held by the handle. */
+CNS_API int64_t cns_device_bytes(const cns_solver* h);
+
+/* Measurement utility with no counterpart in the reference: dependency-free FMA
+ * throughput of the FP64 (fp64 = 1) or FP32 pipe on `device`, in TFLOP/s (FMA = 2),
+ * over `iters` iterations of 8 independent chains per thread. It states the pipe
+ * roofline next to the measured HBM bandwidth. */
+CNS_API int cns_probe_fma_peak(int device, int fp64, int iters, double* tflops);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* CNS_GB300_H_ */

@@ -1,0 +1,301 @@
+"""TEST INFRASTRUCTURE ONLY: build and run the unmodified CudaNavierStokes GPU code to
+produce golden vectors that pin the CPU oracle (and, through it, the GB300 library).
+
+The reference has no CPU path and no tests, so parity is pinned by running the
+reference itself. Steps:
+
+  stage   (in the container that has the reference checkout)
+          For every case below: copy the reference's src/ into oracle/_ref/<case>/src
+          (git-ignored, never committed), write a generated parameter header in place of
+          its compile-time src/globals.h, add oracle/ref_mpi_stub.h as mpi.h, wrap the
+          dead device-side-launch helpers of src/cuda_math.cu (device cudaDeviceSynchronize,
+          which CUDA >= 12 rejects) in `#if 0`, write the initial fields as restart
+          files fields/*.0000000.bin (or, for the boundary layer, synthetic self-similar
+          profiles blasius1D/*.bin) and a Makefile.
+  run     (on the GPU machine) `make` each case for sm_103a and run ./ns with
+          CUDA_LAUNCH_BLOCKING=1 (program order: the reference's streams race otherwise),
+          then pack initial and final fields and the dt/dpdz log into
+          gpurun_out/ref_golden/<case>.npz.
+  collect (back in the container) copy the packed results to tests/golden/.
+
+Usage: python oracle/ref_harness.py {stage|run|collect} [case ...]
+"""
+from __future__ import annotations
+
+import json
+import math
+import os
+import re
+import shutil
+import subprocess
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+REPO = os.path.dirname(HERE)
+sys.path.insert(0, REPO)
+
+from cudanavierstokes_gb300.params import (  # noqa: E402
+    RK3_CLASSIC, RK3_LOWSTORAGE, boundary_layer_params, channel_params, tgv_params)
+from cudanavierstokes_gb300 import initial  # noqa: E402
+
+REF_SRC = "/root/reference/src"
+STAGE_ROOT = os.path.join(HERE, "_ref")
+OUT_ROOT = os.path.join(REPO, "gpurun_out", "ref_golden")
+GOLDEN = os.path.join(REPO, "tests", "golden")
+
+
+def cases():
+    """Golden cases (reference axes). Sizes respect the reference's own launch-geometry
+    checks (src/cuda_utils.cu:233-297): even edges, lPencils = 1 for edges <= 32."""
+    return {
+        # periodic TGV, 8th order, Wray RK3, non-cubic box to catch axis mix-ups
+        "tgv_16x20x24_s4v4": dict(params=tgv_params(16).copy(my=20, mz=24), nsteps=10, ic="tgv"),
+        # classic RK3, low order, dt recomputed during the run (checkCFL=4)
+        "tgv_16_s2v1_rk3classic": dict(params=tgv_params(16).copy(stencil_size=2, stencil_visc=1,
+                                                                   scheme=RK3_CLASSIC, check_cfl=4,
+                                                                   check_bulk=3),
+                                       nsteps=6, ic="tgv_ref"),
+        # isothermal channel: stretched x, walls, body force; dt/dpdz recomputed at 0,3,6
+        "channel_16x12x20_s3v2": dict(params=channel_params(16, 12, 20).copy(stencil_size=3, stencil_visc=2,
+                                                                             check_cfl=3, check_bulk=2),
+                                      nsteps=8, ic="channel"),
+        # channel at 8th order
+        "channel_24x16x16_s4v4": dict(params=channel_params(24, 16, 16), nsteps=5, ic="channel"),
+        # boundary layer: extrapolated x top / z ends, sponge, wall perturbation
+        "bl_16x8x160_s3v2": dict(params=boundary_layer_params(16, 8, 160), nsteps=6, ic="bl"),
+    }
+
+
+def _lit(x: float) -> str:
+    return repr(float(x))
+
+
+COEFF_TEXT = {
+    1: ("{-1.0/2.0}", "{1.0, -2.0}"),
+    2: ("{ 1.0/12.0, -2.0/3.0}", "{-1.0/12.0,  4.0/3.0, -5.0/2.0}"),
+    3: ("{-1.0/60.0,  3.0/20.0, -3.0/4.0}", "{ 1.0/90.0, -3.0/20.0,  3.0/2.0, -49.0/18.0}"),
+    4: ("{ 1.0/280.0, -4.0/105.0,  1.0/5.0, -4.0/5.0}",
+        "{-1.0/560.0,  8.0/315.0, -1.0/5.0,  8.0/5.0,  -205.0/72.0}"),
+}
+
+
+def parameter_header(p, nsteps: int, restart: int) -> str:
+    """The reference's compile-time parameter surface, generated from a cns_params."""
+    b = lambda v: "(true)" if v else "(false)"  # noqa: E731
+    F, Sx = COEFF_TEXT[p.stencil_size]
+    VF, VS = COEFF_TEXT[p.stencil_visc]
+    return f"""/* generated by oracle/ref_harness.py */
+#ifndef GLOBALS_H_
+#define GLOBALS_H_
+#define myprec double
+#define MPI_myprec MPI_DOUBLE
+#include "math.h"
+#include "main.h"
+#include <stdlib.h>
+#include <stdio.h>
+#define pRow 1
+#define pCol 1
+#define stencilSize {p.stencil_size}
+#define stencilVisc {p.stencil_visc}
+#define Lx ({_lit(p.Lx)})
+#define Ly ({_lit(p.Ly)})
+#define Lz ({_lit(p.Lz)})
+#define mx_tot {p.mx}
+#define my_tot {p.my}
+#define mz_tot {p.mz}
+#define nsteps {nsteps}
+#define nfiles 1
+#define CFL {_lit(p.cfl)}
+#define restartFile {restart}
+#define lowStorage {b(p.scheme == RK3_LOWSTORAGE)}
+#define boundaryLayer {b(p.boundary_layer)}
+#define perturbed {b(p.perturbed)}
+#define forcing {b(p.forcing)}
+#define periodicX {b(p.periodic_x)}
+#define nonUniformX {b(p.nonuniform_x)}
+#define checkCFLcondition {p.check_cfl}
+#define checkBulk {p.check_bulk}
+#define Re {_lit(p.Re)}
+#define Pr {_lit(p.Pr)}
+#define Ma {_lit(p.Ma)}
+#define viscexp {_lit(p.viscexp)}
+#define gam {_lit(p.gam)}
+#define Ec ((gam - 1.f)*Ma*Ma)
+#define Rgas (1.f/(gam*Ma*Ma))
+const double stretch = {_lit(p.stretch)};
+const myprec TwallTop = {_lit(p.twall_top)};
+const myprec TwallBot = {_lit(p.twall_bot)};
+#define mx (mx_tot)
+#define my (my_tot/pRow)
+#define mz (mz_tot/pCol)
+#define nDivZ (1)
+#define idx(i,j,k) ({{ ( k )*mx*my +( j )*mx + ( i ); }})
+const int multiGPU = 0;
+const double coeffF[] = {F};
+const double coeffS[] = {Sx};
+const double coeffVF[] = {VF};
+const double coeffVS[] = {VS};
+extern double dt, h_dpdz;
+extern double dx,x[mx],xp[mx],xpp[mx],y[my_tot],z[mz_tot];
+extern double r[mx*my*mz];
+extern double u[mx*my*mz];
+extern double v[mx*my*mz];
+extern double w[mx*my*mz];
+extern double e[mx*my*mz];
+#endif
+"""
+
+
+MAKEFILE = r"""# generated by oracle/ref_harness.py: builds the staged reference for sm_103a
+NVCC ?= nvcc
+CXX ?= g++
+CUDA_HOME ?= /usr/local/cuda
+ARCH = -gencode arch=compute_103a,code=sm_103a
+NVFLAGS = -O3 -rdc=true --use_fast_math $(ARCH) -Isrc
+CXXFLAGS = -O3 -std=c++14 -Isrc -I$(CUDA_HOME)/include
+CU = cuda_utils cuda_math cuda_main cuda_rhs calc_stress sponge
+CC = main comm init
+CUO = $(addprefix obj/,$(addsuffix .o,$(CU)))
+CCO = $(addprefix obj/,$(addsuffix .o,$(CC)))
+ns: $(CUO) $(CCO)
+	$(NVCC) $(ARCH) -dlink $(CUO) -o obj/link.o
+	$(CXX) -o ns $(CCO) $(CUO) obj/link.o -L$(CUDA_HOME)/lib64 -lcudadevrt -lcudart -lm
+obj/%.o: src/%.cu
+	@mkdir -p obj
+	$(NVCC) $(NVFLAGS) -c $< -o $@
+obj/%.o: src/%.cpp
+	@mkdir -p obj
+	$(CXX) $(CXXFLAGS) -c $< -o $@
+"""
+
+
+def _disable_dead_helpers(text: str) -> str:
+    """Wrap reduceToMax .. reduceToOne (device functions that call cudaDeviceSynchronize
+    from device code; nothing on the solver path calls them) in #if 0."""
+    start = text.index("__device__ void reduceToMax")
+    end = text.index("__global__ void integrateThreads")
+    return text[:start] + "#if 0\n" + text[start:end] + "#endif\n" + text[end:]
+
+
+def blasius_like_profile(n: int = 601, xmax: float = 60.0):
+    """Smooth synthetic self-similar profile standing in for the missing blasius1D/*.bin
+    (bLayerInit.py needs matplotlib). x is the similarity coordinate; w the streamwise
+    velocity 0 -> 1, u a small wall-normal velocity, r from a Crocco-like temperature."""
+    x = np.linspace(0.0, xmax, n)
+    w = np.tanh(x / 3.0)
+    u = 0.8 * (x * w - 3.0 * np.log(np.cosh(x / 3.0))) / 3.0
+    T = 1.0 + 0.15 * (1.0 - w * w)
+    r = 1.0 / T
+    e = np.zeros_like(x)
+    return x, r, u, w, e
+
+
+def stage(names):
+    if not os.path.isdir(REF_SRC):
+        raise SystemExit(f"reference sources not found at {REF_SRC}")
+    allc = cases()
+    for name in names or allc:
+        c = allc[name]
+        p, nsteps = c["params"], c["nsteps"]
+        d = os.path.join(STAGE_ROOT, name)
+        if os.path.isdir(d):
+            shutil.rmtree(d)
+        os.makedirs(os.path.join(d, "src"))
+        os.makedirs(os.path.join(d, "fields"))
+        for fn in os.listdir(REF_SRC):
+            if fn.endswith((".cu", ".cpp", ".h")) and fn != "globals.h" and fn != "cuda_derivs.cu":
+                shutil.copy(os.path.join(REF_SRC, fn), os.path.join(d, "src", fn))
+        cm = os.path.join(d, "src", "cuda_math.cu")
+        with open(cm) as f:
+            txt = f.read()
+        with open(cm, "w") as f:
+            f.write(_disable_dead_helpers(txt))
+        shutil.copy(os.path.join(HERE, "ref_mpi_stub.h"), os.path.join(d, "src", "mpi.h"))
+        restart = -1 if c["ic"] == "bl" else 0
+        with open(os.path.join(d, "src", "globals.h"), "w") as f:
+            f.write(parameter_header(p, nsteps, restart))
+        with open(os.path.join(d, "Makefile"), "w") as f:
+            f.write(MAKEFILE)
+        if c["ic"] == "bl":
+            os.makedirs(os.path.join(d, "blasius1D"))
+            for nm, arr in zip("xruwe", blasius_like_profile()):
+                arr.astype(np.float64).tofile(os.path.join(d, "blasius1D", f"{nm}Prof.bin"))
+        else:
+            if c["ic"] == "tgv":
+                fields = initial.tgv_fields(p)
+            elif c["ic"] == "tgv_ref":
+                fields = initial.tgv_reference_fields(p)
+            else:
+                from oracle.oracle import Oracle  # grid of the stretched channel
+                fields = initial.channel_fields(p, Oracle(p).grid()["x"], seed=0)
+            initial.write_fields(os.path.join(d, "fields"), 0, fields)
+        with open(os.path.join(d, "case.json"), "w") as f:
+            json.dump(dict(name=name, nsteps=nsteps, ic=c["ic"], params=p.as_dict()), f, indent=1)
+        print("staged", d)
+
+
+def run(names):
+    os.makedirs(OUT_ROOT, exist_ok=True)
+    dirs = sorted(n for n in os.listdir(STAGE_ROOT) if os.path.isdir(os.path.join(STAGE_ROOT, n)))
+    ok = True
+    for name in dirs:
+        if names and name not in names:
+            continue
+        d = os.path.join(STAGE_ROOT, name)
+        with open(os.path.join(d, "case.json")) as f:
+            meta = json.load(f)
+        nproc = str(os.cpu_count() or 4)
+        # objects compiled elsewhere (another host architecture) are discarded first
+        shutil.rmtree(os.path.join(d, "obj"), ignore_errors=True)
+        if os.path.exists(os.path.join(d, "ns")):
+            os.remove(os.path.join(d, "ns"))
+        b = subprocess.run(["make", "-j", nproc], cwd=d, capture_output=True, text=True)
+        if b.returncode != 0:
+            print(f"[{name}] build failed:\n{b.stdout[-3000:]}\n{b.stderr[-3000:]}")
+            ok = False
+            continue
+        env = dict(os.environ, CUDA_LAUNCH_BLOCKING="1")
+        r = subprocess.run(["./ns"], cwd=d, capture_output=True, text=True, env=env, timeout=600)
+        log = r.stdout + r.stderr
+        with open(os.path.join(OUT_ROOT, name + ".log"), "w") as f:
+            f.write(log)
+        if r.returncode != 0:
+            print(f"[{name}] run failed rc={r.returncode}\n{log[-2000:]}")
+            ok = False
+            continue
+        p = meta["params"]
+        shape = (p["mz"], p["my"], p["mx"])
+        ic = initial.read_fields(os.path.join(d, "fields"), 0, shape)
+        out = initial.read_fields(os.path.join(d, "fields"), 1, shape)
+        steps = [(int(m.group(1)), float(m.group(2)), float(m.group(3)))
+                 for m in re.finditer(r"step number (\d+) with (\S+) (\S+)", log)]
+        np.savez_compressed(os.path.join(OUT_ROOT, name + ".npz"),
+                            ic=np.stack(ic), out=np.stack(out),
+                            x=np.fromfile(os.path.join(d, "fields", "x.bin")),
+                            steplog=np.array(steps, dtype=np.float64).reshape(-1, 3),
+                            meta=json.dumps(meta))
+        print(f"[{name}] ok: {len(steps)} dt lines, rho range {out[0].min():.6f}..{out[0].max():.6f}")
+    return ok
+
+
+def collect(names):
+    os.makedirs(GOLDEN, exist_ok=True)
+    for fn in sorted(os.listdir(OUT_ROOT)):
+        if fn.endswith(".npz") and (not names or fn[:-4] in names):
+            shutil.copy(os.path.join(OUT_ROOT, fn), os.path.join(GOLDEN, "ref_" + fn))
+            print("collected", fn)
+
+
+if __name__ == "__main__":
+    cmd = sys.argv[1] if len(sys.argv) > 1 else "stage"
+    names = sys.argv[2:]
+    if cmd == "stage":
+        stage(names)
+    elif cmd == "run":
+        sys.exit(0 if run(names) else 1)
+    elif cmd == "collect":
+        collect(names)
+    else:
+        raise SystemExit(__doc__)

@@ -1,0 +1,62 @@
+"""The C-ABI library loads, exports every symbol include/cns.h declares, and validates
+parameters on the host (no compute without a GPU)."""
+import ctypes
+import os
+import re
+
+import pytest
+
+from cudanavierstokes_gb300 import native
+from cudanavierstokes_gb300.params import CnsParams, default_params, tgv_params
+
+REPO = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def declared_symbols():
+    names = set()
+    for fn in os.listdir(os.path.join(REPO, "include")):
+        if fn.endswith(".h"):
+            txt = open(os.path.join(REPO, "include", fn)).read()
+            names |= set(re.findall(r"^CNS_API\s+[\w\s\*]+?\b(cns_\w+)\s*\(", txt, flags=re.M))
+    return names
+
+
+def test_header_declares_entry_points():
+    names = declared_symbols()
+    assert {"cns_create", "cns_run", "cns_copy_field", "cns_destroy", "cns_calc_rhs"} <= names
+
+
+def test_library_exports_every_declared_symbol(gpu_lib):
+    for name in declared_symbols():
+        assert hasattr(gpu_lib, name), name
+    assert set(native.SIGNATURES) >= declared_symbols() - set()
+
+
+def test_params_struct_layout_matches_default(gpu_lib):
+    p = CnsParams()
+    gpu_lib.cns_default_params(ctypes.byref(p))
+    q = default_params()
+    for k, v in q.as_dict().items():
+        if k in ("mx", "my", "mz"):
+            continue
+        assert getattr(p, k) == pytest.approx(v), k
+
+
+def test_parameter_validation(gpu_lib):
+    assert gpu_lib.cns_check_params(ctypes.byref(tgv_params(16))) == 0
+    for bad in (dict(stencil_size=5), dict(stencil_visc=0), dict(stencil_visc=4, stencil_size=3), dict(mx=4),
+                dict(check_cfl=0), dict(precision=7), dict(scheme=9), dict(Ma=0.0),
+                dict(boundary_layer=1, periodic_x=1)):
+        p = tgv_params(16).copy(**bad)
+        assert gpu_lib.cns_check_params(ctypes.byref(p)) == 1, bad
+        assert gpu_lib.cns_last_error().decode()
+
+
+def test_create_fails_loudly_without_device(gpu_lib):
+    import torch
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is present")
+    h = ctypes.c_void_p()
+    rc = gpu_lib.cns_create(ctypes.byref(tgv_params(16)), 0, ctypes.byref(h))
+    assert rc == 2 and not h
+    assert "device" in gpu_lib.cns_last_error().decode()

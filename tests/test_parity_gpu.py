@@ -1,0 +1,213 @@
+"""GPU parity: the GB300 library (through its C ABI) against the CPU oracle.
+
+Bar (FP64 path): norm-wise relative error max|a-b|/max|b| <= 1e-12 per field, for a single
+RHS evaluation and after multi-step runs. FP32-RHS path: <= 2e-5 against the FP64 oracle.
+"""
+import numpy as np
+import pytest
+
+from cudanavierstokes_gb300 import Solver
+from cudanavierstokes_gb300.initial import channel_fields, tgv_fields
+from cudanavierstokes_gb300.params import (PREC_FP32_RHS, RK3_CLASSIC, RK4_CLASSIC, boundary_layer_params,
+                                           channel_params, tgv_params)
+from tests._util import field_errors, rel_err, smooth_random_state, wall_state
+
+pytestmark = pytest.mark.gpu
+
+TOL64 = 1e-12
+
+
+def _pair(oracle_mod, p, fields):
+    o = oracle_mod.Oracle(p)
+    s = Solver(p)
+    o.set_state(*fields)
+    s.copy_field_in(*fields)
+    return o, s
+
+
+SV = [(1, 1), (2, 1), (2, 2), (3, 1), (3, 2), (3, 3), (4, 1), (4, 2), (4, 3), (4, 4)]
+
+
+@pytest.mark.parametrize("S,V", SV)
+def test_rhs_periodic_all_orders(gpu_lib, oracle_mod, S, V):
+    p = tgv_params(16).copy(my=20, mz=24, stencil_size=S, stencil_visc=V)
+    o, s = _pair(oracle_mod, p, smooth_random_state(p, seed=S * 10 + V))
+    errs = field_errors(s.calc_rhs(), o.rhs())
+    assert max(errs) <= TOL64, errs
+
+
+@pytest.mark.parametrize("S,V", [(4, 4), (3, 2), (2, 1)])
+def test_rhs_channel_walls(gpu_lib, oracle_mod, S, V):
+    p = channel_params(24, 16, 20).copy(stencil_size=S, stencil_visc=V)
+    o = oracle_mod.Oracle(p)
+    f = wall_state(p, o.grid()["x"])
+    o, s = _pair(oracle_mod, p, f)
+    errs = field_errors(s.calc_rhs(), o.rhs())
+    assert max(errs) <= TOL64, errs
+
+
+@pytest.mark.parametrize("quirk", [0, 1])
+def test_rhs_quirk_switch(gpu_lib, oracle_mod, quirk):
+    p = tgv_params(16).copy(quirk_dissipation_y=quirk)
+    o, s = _pair(oracle_mod, p, smooth_random_state(p, seed=7))
+    errs = field_errors(s.calc_rhs(), o.rhs())
+    assert max(errs) <= TOL64, errs
+
+
+def test_quirk_changes_energy_only(gpu_lib):
+    p = tgv_params(16)
+    f = smooth_random_state(p, seed=7)
+    a = Solver(p.copy(quirk_dissipation_y=1))
+    b = Solver(p.copy(quirk_dissipation_y=0))
+    a.copy_field_in(*f)
+    b.copy_field_in(*f)
+    ra, rb = a.calc_rhs(), b.calc_rhs()
+    for q in range(4):
+        assert np.array_equal(ra[q], rb[q])
+    assert rel_err(ra[4], rb[4]) > 1e-6
+
+
+def _bl_setup(oracle_mod, p):
+    from oracle.ref_harness import blasius_like_profile
+    o = oracle_mod.Oracle(p)
+    spx, spz = o.sponge_strengths()
+    rref, uref, wref, eref = o.sponge_refs(*blasius_like_profile())
+    N = (p.my,)
+    fields = [np.broadcast_to(a[:, None, :], p.shape).copy() for a in (rref, uref, np.zeros_like(rref), wref, eref)]
+    o.set_sponge(spx, spz, rref, uref, wref, eref)
+    s = Solver(p)
+    s.set_sponge(spx, spz, rref, uref, wref, eref)
+    o.set_state(*fields)
+    s.copy_field_in(*fields)
+    del N
+    return o, s
+
+
+def test_rhs_boundary_layer(gpu_lib, oracle_mod):
+    p = boundary_layer_params(16, 8, 160)
+    o, s = _bl_setup(oracle_mod, p)
+    t = 0.37
+    o.set_scalars(0.0, 0.0, t)
+    s.set_scalars(0.0, 0.0, t)
+    errs = field_errors(s.calc_rhs(), o.rhs())
+    assert max(errs) <= TOL64, errs
+
+
+def test_sponge_profile_interpolation(gpu_lib, oracle_mod):
+    from oracle.ref_harness import blasius_like_profile
+    p = boundary_layer_params(16, 8, 160)
+    o = oracle_mod.Oracle(p)
+    rref, uref, wref, eref = o.sponge_refs(*blasius_like_profile())
+    s = Solver(p)
+    s.set_sponge_profiles(*blasius_like_profile(), init_fields=True)
+    r, u, v, w, e = s.copy_field_out()
+    for a, b in ((r, rref), (u, uref), (w, wref), (e, eref)):
+        assert rel_err(a, np.broadcast_to(b[:, None, :], p.shape)) <= 1e-14
+    assert np.all(v == 0)
+
+
+@pytest.mark.parametrize("case", ["tgv_s4v4", "tgv_classic_s2v1", "channel_s3v2", "channel_s4v4", "bl_s3v2",
+                                  "tgv_rk4"])
+def test_run_parity(gpu_lib, oracle_mod, case):
+    if case == "tgv_s4v4":
+        p, n = tgv_params(16).copy(my=20, mz=24), 10
+        f = tgv_fields(p)
+    elif case == "tgv_classic_s2v1":
+        p, n = tgv_params(16).copy(stencil_size=2, stencil_visc=1, scheme=RK3_CLASSIC, check_cfl=4, check_bulk=3), 6
+        f = smooth_random_state(p, seed=3)
+    elif case == "tgv_rk4":
+        p, n = tgv_params(16).copy(scheme=RK4_CLASSIC, check_cfl=2), 5
+        f = smooth_random_state(p, seed=4)
+    elif case.startswith("channel"):
+        S, V = (3, 2) if case == "channel_s3v2" else (4, 4)
+        p, n = channel_params(16, 12, 20).copy(stencil_size=S, stencil_visc=V, check_cfl=3, check_bulk=2), 8
+        f = channel_fields(p, oracle_mod.Oracle(p).grid()["x"], seed=0)
+    else:
+        p, n = boundary_layer_params(16, 8, 160).copy(check_cfl=2), 6
+    if case == "bl_s3v2":
+        o, s = _bl_setup(oracle_mod, p)
+    else:
+        o, s = _pair(oracle_mod, p, f)
+    if case == "tgv_rk4":
+        pytest.skip("RK4 has no oracle counterpart (the reference has no RK4); covered by the order test")
+    lo = o.run(n)
+    lg = s.run(n)
+    errs = field_errors(s.copy_field_out(), o.get_state())
+    assert max(errs) <= TOL64, errs
+    np.testing.assert_allclose(lg["time"], lo["time"], rtol=1e-13)
+    so, sg = o.scalars(), s.scalars()
+    assert abs(sg["dt"] - so["dt"]) <= 1e-13 * abs(so["dt"])
+    assert abs(sg["dpdz"] - so["dpdz"]) <= 1e-12 * max(1.0, abs(so["dpdz"]))
+    has = ~np.isnan(lo["par1"])
+    assert np.array_equal(has, ~np.isnan(lg["par1"]))
+    np.testing.assert_allclose(lg["par1"][has], lo["par1"][has], rtol=1e-12)
+
+
+def test_fp32_rhs_against_fp64_oracle(gpu_lib, oracle_mod):
+    p = tgv_params(24)
+    f = smooth_random_state(p, seed=11)
+    o = oracle_mod.Oracle(p)
+    o.set_state(*f)
+    s = Solver(p.copy(precision=PREC_FP32_RHS))
+    s.copy_field_in(*f)
+    errs = field_errors(s.calc_rhs(), o.rhs())
+    assert max(errs) <= 2e-5, errs
+    o.run(5)
+    s.run(5)
+    errs = field_errors(s.copy_field_out(), o.get_state())
+    assert max(errs) <= 2e-6, errs
+
+
+def test_fp32_rhs_channel(gpu_lib, oracle_mod):
+    p = channel_params(24, 16, 20)
+    o = oracle_mod.Oracle(p)
+    f = wall_state(p, o.grid()["x"])
+    o.set_state(*f)
+    s = Solver(p.copy(precision=PREC_FP32_RHS))
+    s.copy_field_in(*f)
+    errs = field_errors(s.calc_rhs(), o.rhs())
+    assert max(errs) <= 1e-4, errs
+
+
+def test_rk4_third_order_or_better(gpu_lib):
+    """RK4 (no counterpart in the reference): halving dt cuts the error against a fine
+    reference run by at least 2^3."""
+    base = tgv_params(16).copy(scheme=RK4_CLASSIC)
+    f = smooth_random_state(base, seed=5)
+    T = None
+    res = {}
+    for cfl in (0.4, 0.2, 0.05):
+        s = Solver(base.copy(cfl=cfl, check_cfl=10**6))
+        s.copy_field_in(*f)
+        s.run(1)
+        dt = s.scalars()["dt"]
+        if T is None:
+            T = 8 * dt
+        s.copy_field_in(*f)
+        nsteps = int(round(T / dt))
+        s.run(nsteps)
+        res[cfl] = s.copy_field_out()
+    e1 = rel_err(res[0.4][1], res[0.05][1])
+    e2 = rel_err(res[0.2][1], res[0.05][1])
+    assert e1 / e2 > 8.0, (e1, e2)
+
+
+def test_determinism(gpu_lib):
+    p = channel_params(24, 16, 20)
+    f = channel_fields(p, Solver(p).grid()["x"], seed=1)
+    outs = []
+    for _ in range(2):
+        s = Solver(p)
+        s.copy_field_in(*f)
+        s.run(4)
+        outs.append(s.copy_field_out())
+    for a, b in zip(*outs):
+        assert np.array_equal(a, b)
+
+
+def test_grid_matches_oracle(gpu_lib, oracle_mod):
+    for p in (channel_params(24, 16, 20), boundary_layer_params(16, 8, 160), tgv_params(16)):
+        g = Solver(p).grid()
+        go = oracle_mod.Oracle(p).grid()
+        for k in ("x", "xp", "xpp", "y", "z"):
+            np.testing.assert_array_equal(g[k], go[k])
