@@ -1,0 +1,355 @@
+#!/usr/bin/env python
+"""Throughput benchmark of the GB300 time-advance path (prints one JSON line).
+
+Workload: the supersonic isothermal-wall channel 192 x 128 x 160 (reference axes: mx = 128
+wall-normal, my = 160 spanwise, mz = 192 streamwise; stretched walls, constant-mass-flux
+body force), 8th-order stencils (S = V = 4), Wray low-storage RK3, plain FP64.
+A "step" is one RK3 time step of the whole grid (3 stages); the metric is
+Mpoint-steps/s = grid points x steps / second, summed over ranks (replicas only: the
+path is not sharded across GPUs, each rank advances its own channel).
+
+  value       device-resident state, CUDA events on the solver's stream around K steps
+  e2e         the same through the C ABI with pinned host buffers: copy the five fields
+              in, advance K steps, copy them out (host wall clock)
+  roofline    the RHS + stage-update kernel (dominant kernel): its event-timed average
+              launch against the FP64 pipe (measured live) and against HBM
+  cpu_baseline  the CPU oracle (the reference's algorithm restated, OpenMP) on the host
+              cores, on a z-slab of the same channel
+  fp32_rhs    the same workload with the RHS in FP32 (state/accumulation FP64)
+
+--impl reference times the CPU port of the reference's path (the reference itself only
+has a GPU path) on all host cores, on the same workload and metric.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+REPO = os.path.dirname(os.path.abspath(__file__))
+if REPO not in sys.path:
+    sys.path.insert(0, REPO)
+
+METRIC = "Mpoint-steps/s"
+PEAKS_FILE = os.path.join(REPO, "MEASURED_PEAKS.json")
+TRAFFIC_FILE = os.path.join(REPO, "profiles", "rhs_kernel_channel_traffic.txt")
+SLAB_MZ = 24   # CPU sample: full x-y cross-section, 24 streamwise planes
+
+
+def parse_args():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
+    ap.add_argument("--workload", choices=["channel", "tgv"], default="channel")
+    ap.add_argument("--precision", choices=["fp64", "fp32"], default="fp64")
+    ap.add_argument("--no-extras", action="store_true", help="skip fp32/cpu/e2e side measurements")
+    ap.add_argument("--grid", default=None, help="override the grid as MX,MY,MZ (profiling of smaller cases)")
+    return ap.parse_args()
+
+
+def workload(name: str, precision: str, grid=None):
+    from cudanavierstokes_gb300.params import PREC_FP32_RHS, PREC_FP64, channel_params, tgv_params
+    prec = PREC_FP32_RHS if precision == "fp32" else PREC_FP64
+    if grid:
+        mx, my, mz = (int(v) for v in grid.split(","))
+        base = channel_params(mx, my, mz, precision=prec) if name == "channel" else tgv_params(mx, precision=prec)
+        base = base.copy(my=my, mz=mz)
+        return base, f"{name} {mx}x{my}x{mz} (reference axes), 8th order S=V=4, Wray RK3"
+    if name == "channel":
+        p = channel_params(128, 160, 192, precision=prec)
+        desc = ("supersonic isothermal-wall channel 192x128x160 (reference axes mx=128 wall-normal, my=160 span, "
+                "mz=192 stream), Ma 1.5, Re 3000, 8th order S=V=4, Wray RK3")
+    else:
+        p = tgv_params(64, precision=prec)
+        desc = "Taylor-Green vortex 64^3, Ma 0.1, Re 1600, 8th order S=V=4, Wray RK3"
+    return p, desc
+
+
+def initial_state(p, x=None):
+    from cudanavierstokes_gb300.initial import channel_fields, tgv_fields
+    if p.periodic_x:
+        return tgv_fields(p)
+    return channel_fields(p, x, seed=0)
+
+
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled every 200 ms during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        try:
+            fd, self.path = tempfile.mkstemp(suffix=".csv")
+            os.close(fd)
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200", "-f", self.path],
+                                         stdout=subprocess.DEVNULL, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self) -> dict:
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        time.sleep(0.25)
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        rows = []
+        with open(self.path) as f:
+            for line in f:
+                parts = [x.strip() for x in line.split(",")]
+                if len(parts) >= 9:
+                    rows.append(parts)
+        os.remove(self.path)
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+
+        def num(x):
+            try:
+                return float(x)
+            except ValueError:
+                return None
+        sm = [num(r[1]) for r in rows if num(r[1]) is not None]
+        mx = [num(r[2]) for r in rows if num(r[2]) is not None]
+        loaded = [v for v in sm if mx and v >= 0.5 * max(mx)] or sm
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in rows for i in range(4) if r[5 + i].lower() == "active"})
+        return {"sm_mhz": statistics.median(loaded) if loaded else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(rows), "power_w_max": max((num(r[3]) or 0) for r in rows)}
+
+
+def dist_setup():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+        os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+        backend = "nccl" if torch.cuda.is_available() else "gloo"
+        if backend == "nccl":
+            torch.cuda.set_device(local)
+        dist.init_process_group(backend)
+    return world, rank, local
+
+
+def allreduce_max(x: float, world: int) -> float:
+    if world == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    dev = torch.device("cuda", torch.cuda.current_device()) if torch.cuda.is_available() else torch.device("cpu")
+    t = torch.tensor([x], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def barrier(world: int):
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def cpu_sample(p, steps_min: int = 2, seconds: float = 12.0):
+    """Time the CPU oracle on a z-slab of the workload: returns Mpoint-steps/s, threads, text."""
+    from oracle import oracle as orc
+    q = p.copy(mz=SLAB_MZ, Lz=p.Lz * SLAB_MZ / p.mz, precision=0)
+    o = orc.Oracle(q)
+    o.set_state(*initial_state(q, o.grid()["x"]))
+    o.run(1)                       # warm-up step
+    n, t0 = 0, time.perf_counter()
+    while n < steps_min or time.perf_counter() - t0 < seconds:
+        o.run(1)
+        n += 1
+    dt = time.perf_counter() - t0
+    pts = q.npoints
+    return pts * n / dt / 1e6, orc.max_threads(), (f"{n} RK3 steps of a {q.mx}x{q.my}x{q.mz} z-slab of the workload "
+                                                    f"({pts} points, same physics and stencils), {dt:.1f} s")
+
+
+def read_traffic(N: int):
+    """Per-launch DRAM bytes of the RHS kernel from the committed ncu summary (scaled to this
+    grid by points if the capture was taken on a smaller case)."""
+    try:
+        with open(TRAFFIC_FILE) as f:
+            kv = dict(line.split(":", 1) for line in f if ":" in line)
+        b = float(kv["dram_bytes_per_launch"].strip())
+        pts = float(kv["points"].strip())
+        return b * N / pts
+    except Exception:
+        return None
+
+
+def run_reference(args, world, rank):
+    """CPU port of the reference path (the oracle) on all host cores, rank 0 only."""
+    if rank != 0:
+        return
+    from oracle import oracle as orc
+    p, desc = workload(args.workload, "fp64", args.grid)
+    q = p.copy(mz=SLAB_MZ, Lz=p.Lz * SLAB_MZ / p.mz)
+    orc.set_threads(os.cpu_count() or 1)
+    o = orc.Oracle(q)
+    o.set_state(*initial_state(q, o.grid()["x"]))
+    for _ in range(args.warmup):
+        o.run(1)
+    t0 = time.perf_counter()
+    o.run(args.steps)
+    dt = time.perf_counter() - t0
+    v = q.npoints * args.steps / dt / 1e6
+    cores = orc.max_threads()
+    sample = (f"{args.steps} RK3 steps per timed region on a {q.mx}x{q.my}x{q.mz} z-slab of the workload "
+              f"({q.npoints} points, same physics/stencils), CPU restatement of the reference kernels (OpenMP)")
+    line = {"impl": "reference", "metric": METRIC, "value": v, "unit": "Mpoint-steps/s", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": dt / args.steps * 1e3 * p.npoints / q.npoints,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": desc, "grid": [p.mx, p.my, p.mz], "points": p.npoints},
+            "cpu_baseline": {"value": v, "unit": "Mpoint-steps/s", "cores": cores, "kind": "port", "sample": sample},
+            "e2e": {"value": v, "unit": "Mpoint-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def run_gb300(args, world, rank, local):
+    import numpy as np
+    import torch
+
+    from cudanavierstokes_gb300 import Solver, native
+    from cudanavierstokes_gb300 import roofline as rf
+
+    torch.cuda.set_device(local)
+    p, desc = workload(args.workload, args.precision, args.grid)
+    N = p.npoints
+    s = Solver(p, device=local)
+    stream = torch.cuda.Stream(device=local)
+    s.set_stream(stream.cuda_stream)
+    fields = initial_state(p, s.grid()["x"])
+    s.copy_field_in(*fields)
+    s.run(args.warmup, logs=False)
+
+    clocks = ClockSampler(local)
+    barrier(world)
+    torch.cuda.synchronize()
+    clocks.start()
+    l0 = s.kernel_launches
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    s.run(args.steps, logs=False)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    barrier(world)
+    clk = clocks.stop()
+    launches = s.kernel_launches - l0
+    ms = allreduce_max(e0.elapsed_time(e1), world)
+    value = world * N * args.steps / (ms * 1e-3) / 1e6
+
+    # dominant kernel (RHS + stage update), event-timed per launch on the solver's stream
+    ph = s.time_phases(6)
+    S, V = p.stencil_size, p.stencil_visc
+    rhs_s = ph["rhs_ms"] * 1e-3
+    ach_tf = rf.rhs_kernel_flops(S, V) * N / rhs_s / 1e12
+    ach_gbs = rf.RHS_KERNEL_BYTES * N / rhs_s / 1e9
+    t64 = native.ctypes.c_double()
+    native.check(native.lib().cns_probe_fma_peak(local, 1 if args.precision == "fp64" else 0,
+                                                 2000 if args.precision == "fp64" else 20000,
+                                                 native.ctypes.byref(t64)))
+    try:
+        with open(PEAKS_FILE) as f:
+            hbm_peak = float(json.load(f)["hbm_gbs"])
+        hbm_src = "measured (MEASURED_PEAKS.json)"
+    except Exception:
+        hbm_peak, hbm_src = 6800.0, "fallback"
+    traffic = read_traffic(N)
+    roof = {"bound": "fp64" if args.precision == "fp64" else "fp32", "kernel": "k_rhs (RHS x/y/z + body force + "
+            "sponge + RK stage update)", "achieved": ach_tf, "peak": t64.value, "unit": "TFLOP/s",
+            "frac": ach_tf / t64.value, "peak_source": "measured live (FMA-chain probe, cns_probe_fma_peak)",
+            "traffic": traffic, "launch_ms": ph["rhs_ms"],
+            "flops_per_point": rf.rhs_kernel_flops(S, V), "bytes_per_point": rf.RHS_KERNEL_BYTES,
+            "hbm": {"achieved": ach_gbs, "peak": hbm_peak, "unit": "GB/s", "frac": ach_gbs / hbm_peak,
+                    "peak_source": hbm_src},
+            "phase_ms": ph}
+
+    line = {"metric": METRIC, "value": value, "unit": "Mpoint-steps/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64" if args.precision == "fp64" else "f32-rhs/f64-state",
+            "data": "synthetic",
+            "config": {"workload": desc, "grid": [p.mx, p.my, p.mz], "points": N,
+                       "precision": args.precision, "parallelism": f"replicas x{world}",
+                       "l2": "no flush: the working set (~1.3 GB of fields) is 10x the 129 MB L2"},
+            "gpu_launches": launches, "clocks": clk, "roofline": roof}
+
+    if not args.no_extras and rank == 0:
+        # end to end through the C ABI with pinned host buffers
+        pinned = [torch.empty(p.shape, dtype=torch.float64, pin_memory=True).numpy() for _ in range(5)]
+        outs = [torch.empty(p.shape, dtype=torch.float64, pin_memory=True).numpy() for _ in range(5)]
+        for a, f in zip(pinned, fields):
+            a[...] = f
+        s.copy_field_in(*pinned)
+        s.run(1, logs=False)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        s.copy_field_in(*pinned)
+        s.run(args.steps, logs=False)
+        s.copy_field_out(outs)
+        t_e2e = time.perf_counter() - t0
+        line["e2e"] = {"value": N * args.steps / t_e2e / 1e6, "unit": "Mpoint-steps/s",
+                       "h2d_bytes_per_step": 5 * 8 * N / args.steps, "d2h_bytes_per_step": 5 * 8 * N / args.steps,
+                       "what": f"cns_copy_field(0) of 5 pinned host fields + cns_run({args.steps}) + "
+                               "cns_copy_field(1), host wall clock"}
+        if not all(np.isfinite(o).all() for o in outs):
+            line["e2e"]["error"] = "non-finite state"
+        s.close()
+        # FP32-RHS variant of the same workload
+        if args.precision == "fp64":
+            p32, _ = workload(args.workload, "fp32", args.grid)
+            s32 = Solver(p32, device=local)
+            s32.set_stream(stream.cuda_stream)
+            s32.copy_field_in(*fields)
+            s32.run(args.warmup, logs=False)
+            torch.cuda.synchronize()
+            e0.record(stream)
+            s32.run(args.steps, logs=False)
+            e1.record(stream)
+            torch.cuda.synchronize()
+            ms32 = e0.elapsed_time(e1)
+            ph32 = s32.time_phases(6)
+            line["fp32_rhs"] = {"value": N * args.steps / (ms32 * 1e-3) / 1e6, "unit": "Mpoint-steps/s",
+                                "ms_per_step": ms32 / args.steps, "phase_ms": ph32,
+                                "speedup_vs_fp64": (ms / ms32)}
+            s32.close()
+        # CPU baseline (oracle) on the host cores
+        v, cores, sample = cpu_sample(p)
+        line["cpu_baseline"] = {"value": v, "unit": "Mpoint-steps/s", "cores": cores, "kind": "port",
+                                "sample": sample}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+
+
+def main():
+    args = parse_args()
+    world, rank, local = dist_setup()
+    if args.impl == "reference":
+        run_reference(args, world, rank)
+    else:
+        run_gb300(args, world, rank, local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -658,6 +658,36 @@ int cns_set_scalars(cns_solver* h, double dt, double dpdz, double time, int64_t 
     return CNS_OK;
 }
 
+int cns_time_phases(cns_solver* h, int nstages, double* ms) {
+    if (!h || !ms || nstages < 1) return fail(CNS_ERR_INVALID, "bad arguments");
+    if (!h->initialized) return fail(CNS_ERR_STATE, "no field has been copied in");
+    CK(cudaSetDevice(h->device));
+    cudaEvent_t ev[4];
+    for (int i = 0; i < 4; i++) CK(cudaEventCreate(&ev[i]));
+    double acc[3] = {0, 0, 0};
+    int rc = CNS_OK;
+    for (int s = 0; s < nstages && !rc; s++) {
+        const int st = s % 3;
+        CK(cudaEventRecord(ev[0], h->stream));
+        if ((rc = state_any(h, 0, nullptr))) break;
+        CK(cudaEventRecord(ev[1], h->stream));
+        if ((rc = grad_any(h))) break;
+        CK(cudaEventRecord(ev[2], h->stream));
+        if ((rc = rhs_any(h, ST_LS, WRAY_A[st], WRAY_B[st]))) break;
+        CK(cudaEventRecord(ev[3], h->stream));
+        CK(cudaEventSynchronize(ev[3]));
+        for (int i = 0; i < 3; i++) {
+            float t = 0.f;
+            CK(cudaEventElapsedTime(&t, ev[i], ev[i + 1]));
+            acc[i] += t;
+        }
+    }
+    for (int i = 0; i < 4; i++) cudaEventDestroy(ev[i]);
+    if (rc) return rc;
+    for (int i = 0; i < 3; i++) ms[i] = acc[i] / nstages;
+    return CNS_OK;
+}
+
 int64_t cns_kernel_launches(const cns_solver* h) { return h ? h->launches : 0; }
 
 int64_t cns_device_bytes(const cns_solver* h) { return h ? h->bytes : 0; }

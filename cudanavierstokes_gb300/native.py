@@ -33,6 +33,7 @@ SIGNATURES = {
     "cns_calc_rhs": (ctypes.c_int, [_vp] + [_dp] * 5),
     "cns_get_scalars": (ctypes.c_int, [_vp] + [_dp] * 3),
     "cns_set_scalars": (ctypes.c_int, [_vp, ctypes.c_double, ctypes.c_double, ctypes.c_double, ctypes.c_int64]),
+    "cns_time_phases": (ctypes.c_int, [_vp, ctypes.c_int, _dp]),
     "cns_kernel_launches": (ctypes.c_int64, [_vp]),
     "cns_device_bytes": (ctypes.c_int64, [_vp]),
     "cns_probe_fma_peak": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, ctypes.c_int, _dp]),

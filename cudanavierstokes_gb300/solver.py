@@ -115,6 +115,12 @@ class Solver:
     def set_scalars(self, dt: float, dpdz: float, time: float, step: int = -1) -> None:
         native.check(native.lib().cns_set_scalars(self._h, float(dt), float(dpdz), float(time), int(step)))
 
+    def time_phases(self, nstages: int = 3) -> dict:
+        """Per-phase device time (ms) averaged over nstages low-storage stages."""
+        ms = np.zeros(3)
+        native.check(native.lib().cns_time_phases(self._h, int(nstages), _ptr(ms)))
+        return dict(state_ms=float(ms[0]), grad_ms=float(ms[1]), rhs_ms=float(ms[2]))
+
     @property
     def kernel_launches(self) -> int:
         return int(native.lib().cns_kernel_launches(self._h))

@@ -23,6 +23,21 @@ def field_errors(A, B):
     return [rel_err(a, b) for a, b in zip(A, B)]
 
 
+def state_errors(A, B):
+    """Per-field errors of a (rho, u, v, w, rhoE) state: rho and rhoE relative to their own
+    maximum; the velocity components relative to the largest velocity component of B (a
+    component that stays near zero, e.g. the spanwise velocity of a boundary layer, has no
+    meaningful scale of its own)."""
+    vscale = max(float(np.max(np.abs(b))) for b in B[1:4])
+    out = []
+    for q, (a, b) in enumerate(zip(A, B)):
+        if q in (1, 2, 3):
+            out.append(float(np.max(np.abs(np.asarray(a) - np.asarray(b)))) / vscale)
+        else:
+            out.append(rel_err(a, b))
+    return out
+
+
 def smooth_random_state(p, seed: int = 1, amp: float = 0.05):
     """A smooth, fully three-dimensional state with O(1) variation of every field: a few
     seeded periodic Fourier modes on top of a uniform flow at rest (rho ~ 1, T ~ 1)."""

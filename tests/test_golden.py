@@ -1,0 +1,31 @@
+"""Pin the CPU oracle to the reference: run every golden case (initial state, parameters
+and step count recorded from a run of the unmodified CudaNavierStokes GPU code) and compare
+the final state, the grid and the printed dt sequence."""
+import numpy as np
+import pytest
+
+from tests import golden_cases
+from tests._util import state_errors
+
+TOL = 1e-12
+
+
+def test_golden_cases_present():
+    assert len(golden_cases.names()) >= 5
+
+
+@pytest.mark.parametrize("name", golden_cases.names())
+def test_oracle_matches_reference(oracle_mod, name):
+    c = golden_cases.load(name)
+    p = c["params"]
+    o = oracle_mod.Oracle(p)
+    np.testing.assert_allclose(o.grid()["x"], c["x"], rtol=0, atol=1e-14)
+    if c["kind"] == "bl":
+        o.set_sponge(*golden_cases.sponge_from_ic(c, o.sponge_strengths()))
+    o.set_state(*c["ic"])
+    logs = o.run(c["nsteps"])
+    errs = state_errors(o.get_state(), c["out"])
+    assert max(errs) <= TOL, errs
+    # the reference prints dt with 7 significant digits at every dt update
+    for step, dt, _ in c["steplog"]:
+        assert abs(logs["dt"][int(step)] - dt) <= 5e-7 * dt
