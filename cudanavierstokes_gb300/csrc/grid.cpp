@@ -94,8 +94,12 @@ int build_grid(const cns_params& p, HostGrid& g) {
     for (int d = 0; d < 3; d++) {
         const double inv = d == 0 ? g.dx : d == 1 ? g.dy : g.dz;
         const double inv2 = d == 0 ? g.d2x : d == 1 ? g.d2y : g.d2z;
-        for (int k = 0; k < 5; k++) g.c1S[d][k] = g.c1V[d][k] = g.c2V[d][k] = 0.0;
-        for (int k = 1; k <= S; k++) g.c1S[d][k] = -cF[S - k] * inv;
+        for (int k = 0; k < 5; k++) g.c1S[d][k] = g.c1V[d][k] = g.c2V[d][k] = g.fq[d][k] = g.fc[d][k] = 0.0;
+        for (int k = 1; k <= S; k++) {
+            g.c1S[d][k] = -cF[S - k] * inv;
+            g.fq[d][k] = 0.5 * g.c1S[d][k];
+            g.fc[d][k] = 0.25 * g.c1S[d][k];
+        }
         for (int k = 1; k <= V; k++) g.c1V[d][k] = -cVF[V - k] * inv;
         for (int k = 0; k <= V; k++) g.c2V[d][k] = cVS[V - k] * inv2;
     }

@@ -8,7 +8,7 @@ namespace cns {
 struct HostGrid {
     std::vector<double> x, xp, xpp, y, z, dxv, wvol, cvsx;
     double dx, dy, dz, d2x, d2y, d2z;   // inverse spacings (d_dx ... of the reference)
-    double c1S[3][5], c1V[3][5], c2V[3][5];
+    double c1S[3][5], c1V[3][5], c2V[3][5], fq[3][5], fc[3][5];
 };
 
 void fd_coeffs(int n, double F[4], double Sc[5]);

@@ -25,7 +25,7 @@ __global__ void __launch_bounds__(128) k_state(Geom g, Phys ph, StateIn q, Deriv
     if (i >= g.mx || j >= g.my) return;
     const long long c = g.at(i, j, k);
     const double rr = q.r[c], uu = q.u[c], vv = q.v[c], ww = q.w[c], ee = q.e[c];
-    const double inv = 1.0 / rr;
+    const double inv = rcp_nr(rr);
     const double en = ee * inv - 0.5 * (uu * uu + vv * vv + ww * ww);
     const double T = ph.cvInv * en;
     const double pr = rr * ph.Rgas * T;

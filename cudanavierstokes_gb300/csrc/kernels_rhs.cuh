@@ -50,10 +50,14 @@ __device__ __forceinline__ R d2x_nu(const R* __restrict__ f, long long c, const 
     return s;
 }
 
+// Contribution of direction DIR (deviceRHSX/Y/Z). The viscous momentum terms
+// (grad mu . s + mu lap u + mu/3 grad theta) of all directions are summed in W[] and the
+// dissipation / conduction in diss / cond, so the energy equation's u_i W_i work term
+// and the mu multiplications are applied once per point instead of once per direction.
 template <typename R, int S, int V, int DIR>
 __device__ __forceinline__ void rhs_direction(const Geom& g, const CoefT<R>& cf, const RhsIn<R>& in, long long c,
-                                              int i, const R (&Gr)[9], R th0, R m0, R l0, R u0, R v0, R w0, R r0,
-                                              R h0, int quirk, R (&acc)[5]) {
+                                              int i, const R (&Gr)[9], R th0, R m0, R m3, R l0, R u0, R v0, R w0,
+                                              R r0, R h0, int quirk, R (&acc)[5], R (&W)[3], R& diss, R& cond) {
     const long long st = DIR == 0 ? 1LL : (DIR == 1 ? g.P : g.PS);
     const bool nux = (DIR == 0) && g.nonuniform_x;
     const R xpi = nux ? cf.xp[i] : (R)1;
@@ -66,12 +70,14 @@ __device__ __forceinline__ void rhs_direction(const Geom& g, const CoefT<R>& cf,
 #pragma unroll
     for (int q = 0; q < 3; q++)
         tau[q] = (q == DIR) ? (R)2 * Gr[3 * DIR + q] - (R)(2. / 3.) * th0 : Gr[3 * DIR + q] + Gr[3 * q + DIR];
-    // viscous dissipation tau_{DIR,c} d u_c / d x_DIR (y: tau_yz * dv/dz with the quirk, cuda_rhs.cu:175)
+    // viscous dissipation tau_{DIR,c} d u_c / d x_DIR / mu (y: tau_yz dv/dz with the quirk, cuda_rhs.cu:175)
     const R dw = (DIR == 1 && quirk) ? Gr[7] : Gr[3 * DIR + 2];
-    R e = m0 * (tau[0] * Gr[3 * DIR + 0] + tau[1] * Gr[3 * DIR + 1] + tau[2] * dw);
+    diss = fma(tau[0], Gr[3 * DIR + 0], diss);
+    diss = fma(tau[1], Gr[3 * DIR + 1], diss);
+    diss = fma(tau[2], dw, diss);
 
+    // d mu/dx s_{DIR,c} + mu d2 u_c/dx2
     const R dmu = d1<R, V>(in.m, c, st, c1V) * xpi;
-    tau[0] *= dmu; tau[1] *= dmu; tau[2] *= dmu;
     R d2uu, d2vv, d2ww, d2tt;
     if (nux) {
         d2uu = d2x_nu<R, V>(in.u, c, cf.cvsx, g.mx, i);
@@ -84,26 +90,27 @@ __device__ __forceinline__ void rhs_direction(const Geom& g, const CoefT<R>& cf,
         d2ww = d2u<R, V>(in.w, c, st, c2V);
         d2tt = d2u<R, V>(in.t, c, st, c2V);
     }
-    tau[0] = fma(d2uu, m0, tau[0]);
-    tau[1] = fma(d2vv, m0, tau[1]);
-    tau[2] = fma(d2ww, m0, tau[2]);
-    e = e + u0 * tau[0] + v0 * tau[1] + w0 * tau[2];
+    W[0] = fma(tau[0], dmu, fma(d2uu, m0, W[0]));
+    W[1] = fma(tau[1], dmu, fma(d2vv, m0, W[1]));
+    W[2] = fma(tau[2], dmu, fma(d2ww, m0, W[2]));
     // heat conduction: lambda d2T + dlambda dT
-    e = fma(d2tt, l0, e);
     const R dl = d1<R, V>(in.l, c, st, c1V) * xpi;
     const R dt = d1<R, V>(in.t, c, st, c1V) * xpi;
-    e = fma(dt, dl, e);
-    // mu/3 d(theta) and the pressure gradient on the DIR momentum
+    cond = fma(d2tt, l0, cond);
+    cond = fma(dt, dl, cond);
+    // mu/3 d(theta) on the DIR momentum (and its work), pressure gradient
     const R dth = d1<R, V>(in.dil, c, st, c1V) * xpi;
     const R dp = d1<R, S>(in.p, c, st, c1S) * xpi;
-    const R mth = m0 * dth / (R)3.0;
-    const R un = DIR == 0 ? u0 : (DIR == 1 ? v0 : w0);
-    tau[DIR] = tau[DIR] + mth - dp;
-    e = fma(mth, un, e);
+    W[DIR] = fma(m3, dth, W[DIR]);
 
-    // split-form convective derivatives, telescoped (see file comment)
-    const R* gv = DIR == 0 ? in.u : (DIR == 1 ? in.v : in.w);
-    R fr = 0, fu = 0, fv = 0, fw = 0, fe = 0;
+    // split-form convective derivatives, telescoped (see file comment); with a uniform
+    // spacing the flux weights already carry 1/2 or 1/4 and 1/dx, so they accumulate
+    // straight into the RHS
+    const R un = DIR == 0 ? u0 : (DIR == 1 ? v0 : w0);
+    R fr = nux ? (R)0 : acc[0], fu = nux ? (R)0 : acc[1], fv = nux ? (R)0 : acc[2], fw = nux ? (R)0 : acc[3],
+      fe = nux ? (R)0 : acc[4];
+    const R* fq = cf.fq[DIR];
+    const R* fcb = cf.fc[DIR];
 #pragma unroll
     for (int l = 1; l <= S; l++) {
         const long long o = l * st;
@@ -114,22 +121,25 @@ __device__ __forceinline__ void rhs_direction(const Geom& g, const CoefT<R>& cf,
         const R hm = ld(in.h, c - o), hp = ld(in.h, c + o);
         const R gm = DIR == 0 ? um : (DIR == 1 ? vm : wm);
         const R gp = DIR == 0 ? up : (DIR == 1 ? vp : wp);
-        (void)gv;
         const R Qm = (rm + r0) * (gm + un);
         const R Qp = (r0 + rp) * (un + gp);
-        const R a = c1S[l];
-        fr = fma(a, Qm - Qp, fr);
-        fu = fma(a, Qm * (um + u0) - Qp * (u0 + up), fu);
-        fv = fma(a, Qm * (vm + v0) - Qp * (v0 + vp), fv);
-        fw = fma(a, Qm * (wm + w0) - Qp * (w0 + wp), fw);
-        fe = fma(a, Qm * (hm + h0) - Qp * (h0 + hp), fe);
+        const R a = fcb[l];
+        fr = fma(fq[l], Qm - Qp, fr);
+        fu = fma(a, fma(Qm, um + u0, -Qp * (u0 + up)), fu);
+        fv = fma(a, fma(Qm, vm + v0, -Qp * (v0 + vp)), fv);
+        fw = fma(a, fma(Qm, wm + w0, -Qp * (w0 + wp)), fw);
+        fe = fma(a, fma(Qm, hm + h0, -Qp * (h0 + hp)), fe);
     }
-    const R cq = (R)0.5 * xpi, cc = (R)0.25 * xpi;
-    acc[0] = fma(cq, fr, acc[0]);
-    acc[1] = acc[1] + tau[0] + cc * fu;
-    acc[2] = acc[2] + tau[1] + cc * fv;
-    acc[3] = acc[3] + tau[2] + cc * fw;
-    acc[4] = acc[4] + e + cc * fe;
+    if (nux) {
+        acc[0] = fma(xpi, fr, acc[0]);
+        acc[1] = fma(xpi, fu, acc[1]);
+        acc[2] = fma(xpi, fv, acc[2]);
+        acc[3] = fma(xpi, fw, acc[3]);
+        acc[4] = fma(xpi, fe, acc[4]);
+    } else {
+        acc[0] = fr; acc[1] = fu; acc[2] = fv; acc[3] = fw; acc[4] = fe;
+    }
+    acc[1 + DIR] -= dp;
 }
 
 template <typename R, int S, int V>
@@ -146,10 +156,17 @@ __global__ void __launch_bounds__(128) k_rhs(Geom g, CoefT<R> cf, RhsIn<R> in, U
     for (int q = 0; q < 9; q++) Gr[q] = ld(in.g[q], c);
     const R th0 = ld(in.dil, c), m0 = ld(in.m, c), l0 = ld(in.l, c);
     const R u0 = ld(in.u, c), v0 = ld(in.v, c), w0 = ld(in.w, c), r0 = ld(in.r, c), h0 = ld(in.h, c);
+    const R m3 = m0 * (R)(1.0 / 3.0);
     R acc[5] = {0, 0, 0, 0, 0};
-    rhs_direction<R, S, V, 0>(g, cf, in, c, i, Gr, th0, m0, l0, u0, v0, w0, r0, h0, quirk, acc);
-    rhs_direction<R, S, V, 1>(g, cf, in, c, i, Gr, th0, m0, l0, u0, v0, w0, r0, h0, quirk, acc);
-    rhs_direction<R, S, V, 2>(g, cf, in, c, i, Gr, th0, m0, l0, u0, v0, w0, r0, h0, quirk, acc);
+    R W[3] = {0, 0, 0};
+    R diss = 0, cond = 0;
+    rhs_direction<R, S, V, 0>(g, cf, in, c, i, Gr, th0, m0, m3, l0, u0, v0, w0, r0, h0, quirk, acc, W, diss, cond);
+    rhs_direction<R, S, V, 1>(g, cf, in, c, i, Gr, th0, m0, m3, l0, u0, v0, w0, r0, h0, quirk, acc, W, diss, cond);
+    rhs_direction<R, S, V, 2>(g, cf, in, c, i, Gr, th0, m0, m3, l0, u0, v0, w0, r0, h0, quirk, acc, W, diss, cond);
+    acc[1] += W[0];
+    acc[2] += W[1];
+    acc[3] += W[2];
+    acc[4] += fma(m0, diss, cond) + fma(u0, W[0], fma(v0, W[1], w0 * W[2]));
 
     // ---- FP64 from here: body force, sponge, stage update ----
     const double dpdz = scal[SC_DPDZ];
@@ -204,7 +221,7 @@ __global__ void __launch_bounds__(128) k_rhs(Geom g, CoefT<R> cf, RhsIn<R> in, U
             }
         }
     }
-    const double inv = 1.0 / qn[0];
+    const double inv = rcp_nr(qn[0]);
     up.qout.r[c] = qn[0];
     up.qout.u[c] = qn[1] * inv;
     up.qout.v[c] = qn[2] * inv;

@@ -413,6 +413,8 @@ int cns_create(const cns_params* pin, int device, cns_solver** out) {
             h->cf64.c1S[d][k] = h->hg.c1S[d][k]; h->cf64.c1V[d][k] = h->hg.c1V[d][k]; h->cf64.c2V[d][k] = h->hg.c2V[d][k];
             h->cf32.c1S[d][k] = (float)h->hg.c1S[d][k]; h->cf32.c1V[d][k] = (float)h->hg.c1V[d][k];
             h->cf32.c2V[d][k] = (float)h->hg.c2V[d][k];
+            h->cf64.fq[d][k] = h->hg.fq[d][k]; h->cf64.fc[d][k] = h->hg.fc[d][k];
+            h->cf32.fq[d][k] = (float)h->hg.fq[d][k]; h->cf32.fc[d][k] = (float)h->hg.fc[d][k];
         }
 
     CK(cudaStreamCreateWithFlags(&h->own_stream, cudaStreamNonBlocking));

@@ -193,6 +193,21 @@ CNS_API int64_t cns_kernel_launches(const cns_solver* h);
 /* Device bytes held by the handle. */
 CNS_API int64_t cns_device_bytes(const cns_solver* h);
 
+/* Stateless device reductions of a caller-owned state, the reference's calcTimeStep
+ * (deviceCalcDt + hostReduceToMin, src/calc_stress.cu:122-160, src/cuda_math.cu:308-333)
+ * and the volume integrals of calcPressureGrad / calcBulk (src/calc_stress.cu:98-201,
+ * hostVolumeIntegral src/cuda_math.cu:335-359). Inputs are device pointers to contiguous
+ * [k][j][i] FP64 fields of mx*my*mz points: rho, primitive u, v, w, rhoE and the dynamic
+ * viscosity mu; dxv[mx] (device) the x cell widths, dy, dz the uniform y/z spacings.
+ * out (device, 5 doubles): [0] CFL time step min(cfl / max(convective, viscous rate)),
+ * [1] sum rho dV, [2] sum rho w dV, [3] sum rhoE dV, [4] sum |u|^2 dV, dV = dxv*dy*dz.
+ * Like the reference, it allocates its scratch (5*mz doubles) with cudaMalloc per call;
+ * work is issued on `stream` (a cudaStream_t, NULL = legacy default) and the call
+ * returns after the stream has finished. */
+CNS_API int cns_reduce_state(int mx, int my, int mz, const double* r, const double* u, const double* v,
+                             const double* w, const double* e, const double* mu, const double* dxv, double dy,
+                             double dz, double gam, double cfl, double* out, void* stream);
+
 /* Measurement utility with no counterpart in the reference: dependency-free FMA
  * throughput of the FP64 (fp64 = 1) or FP32 pipe on `device`, in TFLOP/s (FMA = 2),
  * over `iters` iterations of 8 independent chains per thread. It states the pipe

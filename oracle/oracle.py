@@ -35,7 +35,10 @@ def build(force: bool = False) -> str:
     if not force and os.path.exists(LIB_PATH) and os.path.getmtime(LIB_PATH) >= os.path.getmtime(SRC):
         return LIB_PATH
     tmp = LIB_PATH + f".tmp{os.getpid()}"
-    cmd = ["g++", "-O2", "-fopenmp", "-fPIC", "-shared", "-std=c++17", "-o", tmp, SRC]
+    # -fno-ipa-modref: GCC 13.3 on aarch64 at -O1/-O2 drops the ghost-cell stores of the
+    # line extrapolation helpers (boundary-layer top boundary) under its interprocedural
+    # mod/ref analysis; bisected on the Grace host (x86_64 builds are unaffected).
+    cmd = ["g++", "-O2", "-fno-ipa-modref", "-fopenmp", "-fPIC", "-shared", "-std=c++17", "-o", tmp, SRC]
     subprocess.run(cmd, check=True)
     os.replace(tmp, LIB_PATH)
     return LIB_PATH
