@@ -30,12 +30,21 @@ __global__ void __launch_bounds__(128) k_state(Geom g, Phys ph, StateIn q, Deriv
     const double T = ph.cvInv * en;
     const double pr = rr * ph.Rgas * T;
     const double hh = (ee + pr) * inv;
-    const double suth = ph.vexp_is_one ? T : pow(T, ph.vexp);
     o.t[c] = (R)T;
     o.p[c] = (R)pr;
     o.h[c] = (R)hh;
-    o.m[c] = (R)(suth * ph.invRe);
-    o.l[c] = (R)(suth * ph.clam);
+    if constexpr (sizeof(R) == 4) {
+        // FP32-RHS mode: transport properties are RHS inputs, evaluated in FP32 from the
+        // FP64 temperature
+        const float Tf = (float)T;
+        const float suth = ph.vexp_is_one ? Tf : powf(Tf, (float)ph.vexp);
+        o.m[c] = suth * (float)ph.invRe;
+        o.l[c] = suth * (float)ph.clam;
+    } else {
+        const double suth = ph.vexp_is_one ? T : pow(T, ph.vexp);
+        o.m[c] = (R)(suth * ph.invRe);
+        o.l[c] = (R)(suth * ph.clam);
+    }
     if (o.r32) {
         o.r32[c] = (R)rr; o.u32[c] = (R)uu; o.v32[c] = (R)vv; o.w32[c] = (R)ww;
     }

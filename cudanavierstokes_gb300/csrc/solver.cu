@@ -57,6 +57,13 @@ int fail(int code, const char* fmt, ...) {
 
 }  // namespace
 
+namespace cns {
+int set_error(int code, const char* msg) {
+    g_err = msg ? msg : "";
+    return code;
+}
+}  // namespace cns
+
 struct cns_solver {
     cns_params p{};
     int device = 0;
