@@ -37,6 +37,7 @@ SIGNATURES = {
     "cns_kernel_launches": (ctypes.c_int64, [_vp]),
     "cns_device_bytes": (ctypes.c_int64, [_vp]),
     "cns_reduce_state": (ctypes.c_int, [ctypes.c_int] * 3 + [_vp] * 7 + [ctypes.c_double] * 4 + [_vp, _vp]),
+    "cns_reduce_state_noalloc": (ctypes.c_int, [ctypes.c_int] * 3 + [_vp] * 7 + [ctypes.c_double] * 4 + [_vp, _vp]),
     "cns_probe_fma_peak": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, ctypes.c_int, _dp]),
 }
 

@@ -208,6 +208,23 @@ CNS_API int cns_reduce_state(int mx, int my, int mz, const double* r, const doub
                              const double* w, const double* e, const double* mu, const double* dxv, double dy,
                              double dz, double gam, double cfl, double* out, void* stream);
 
+/* Allocation-free variant of cns_reduce_state; it has no counterpart in the reference.
+ * For callers that may not call cudaMalloc: work issued while a stream is captured into
+ * a CUDA graph, code whose device memory belongs to another allocator or a fixed HBM
+ * budget, and loops that must not block on allocation. Same arguments and results as
+ * cns_reduce_state, but the per-plane partials live in a fixed device array of
+ * 5 * CNS_NOALLOC_MAX_PLANES doubles (160 KiB, held by every GPU that loads the library)
+ * and the call neither allocates nor frees memory nor synchronises: results are ready
+ * when `stream` reaches this point. mz > CNS_NOALLOC_MAX_PLANES is rejected with
+ * CNS_ERR_INVALID. The first call on a device looks up the array's device address (a
+ * one-time cudaGetSymbolAddress with that device current); make that first call before
+ * any stream capture. All calls share the array: calls whose work overlaps on the GPU
+ * race and must be serialised by the caller. */
+#define CNS_NOALLOC_MAX_PLANES 4096
+CNS_API int cns_reduce_state_noalloc(int mx, int my, int mz, const double* r, const double* u, const double* v,
+                                     const double* w, const double* e, const double* mu, const double* dxv,
+                                     double dy, double dz, double gam, double cfl, double* out, void* stream);
+
 /* Measurement utility with no counterpart in the reference: dependency-free FMA
  * throughput of the FP64 (fp64 = 1) or FP32 pipe on `device`, in TFLOP/s (FMA = 2),
  * over `iters` iterations of 8 independent chains per thread. It states the pipe
