@@ -1,0 +1,45 @@
+// batch_launch.cuh -- cooperative launch and occupancy query of the batched stage kernel.
+#pragma once
+#include "batch_kernel.cuh"
+
+namespace cns {
+
+template <typename R, int S, int V>
+cudaError_t batch_launch_t(dim3 grid, dim3 block, const BatchInst<R>* tab, const BatchCtl* ctl, int cur, int kind,
+                           double a, double b, int stage0, int quirk, unsigned* bar, int* err, cudaStream_t s) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = grid;
+    cfg.blockDim = block;
+    cfg.dynamicSmemBytes = 0;
+    cfg.stream = s;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeCooperative;
+    attr[0].val.cooperative = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    return cudaLaunchKernelEx(&cfg, k_batch_stage<R, S, V>, tab, ctl, cur, kind, a, b, stage0, quirk, bar, err);
+}
+
+template <typename R>
+cudaError_t batch_launch_dispatch(int S, int V, dim3 grid, dim3 block, const BatchInst<R>* tab, const BatchCtl* ctl,
+                                  int cur, int kind, double a, double b, int stage0, int quirk, unsigned* bar,
+                                  int* err, cudaStream_t s) {
+#define CNS_BL(SS, VV) \
+    if (S == SS && V == VV) return batch_launch_t<R, SS, VV>(grid, block, tab, ctl, cur, kind, a, b, stage0, quirk, bar, err, s);
+    CNS_BL(1, 1) CNS_BL(2, 1) CNS_BL(2, 2) CNS_BL(3, 1) CNS_BL(3, 2) CNS_BL(3, 3)
+    CNS_BL(4, 1) CNS_BL(4, 2) CNS_BL(4, 3) CNS_BL(4, 4)
+#undef CNS_BL
+    return cudaErrorInvalidValue;
+}
+
+template <typename R>
+cudaError_t batch_occ_dispatch(int S, int V, int threads, int* nb) {
+#define CNS_BO(SS, VV) \
+    if (S == SS && V == VV) return cudaOccupancyMaxActiveBlocksPerMultiprocessor(nb, k_batch_stage<R, SS, VV>, threads, 0);
+    CNS_BO(1, 1) CNS_BO(2, 1) CNS_BO(2, 2) CNS_BO(3, 1) CNS_BO(3, 2) CNS_BO(3, 3)
+    CNS_BO(4, 1) CNS_BO(4, 2) CNS_BO(4, 3) CNS_BO(4, 4)
+#undef CNS_BO
+    return cudaErrorInvalidValue;
+}
+
+}  // namespace cns

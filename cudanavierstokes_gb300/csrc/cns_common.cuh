@@ -16,7 +16,7 @@ namespace cns {
 enum XBC { XBC_PER = 0, XBC_WALL = 1, XBC_BL = 2 };
 
 // indices into the device scalar block
-enum { SC_DT = 0, SC_DPDZ = 1, SC_TIME = 2, SC_NONFINITE = 3, SC_COUNT = 8 };
+enum { SC_DT = 0, SC_DPDZ = 1, SC_TIME = 2, SC_NONFINITE = 3, SC_STEP = 4, SC_COUNT = 8 };
 
 struct Geom {
     int mx, my, mz, G;

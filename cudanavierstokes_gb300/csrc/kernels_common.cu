@@ -2,216 +2,41 @@
 // layout conversion. The RHS/stage kernel lives in kernels_rhs.cuh.
 #include "cns_common.cuh"
 #include "cns_internal.h"
+#include "kernels_point.cuh"
 
 namespace cns {
 
-// ---------------------------------------------------------------------------------
-// State recovery (calcState, src/cuda_main.cu:218-242): T, p, H, mu, lambda from
-// rho, u, v, w, rhoE. FP64 arithmetic; results stored as R. In FP32-RHS mode the
-// stencil copies of rho, u, v, w are also written as FP32.
-// Stage 0 of a step also advances the simulation time by dt (deviceAdvanceTime).
-// ---------------------------------------------------------------------------------
+// Single-solver kernels: thin grids over the per-point bodies of kernels_point.cuh.
 template <typename R>
 __global__ void __launch_bounds__(128) k_state(Geom g, Phys ph, StateIn q, DerivedOut<R> o, double* scal,
-                                               int advance_time, double* time_log) {
+                                               int adv, double* time_log) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     const int j = blockIdx.y * blockDim.y + threadIdx.y;
     const int k = blockIdx.z;
-    if (advance_time && i == 0 && j == 0 && k == 0) {
-        double tn = scal[SC_TIME] + scal[SC_DT];
-        scal[SC_TIME] = tn;
-        if (time_log) *time_log = tn;
-    }
+    if (adv && i == 0 && j == 0 && k == 0) advance_time(scal, time_log);
     if (i >= g.mx || j >= g.my) return;
-    const long long c = g.at(i, j, k);
-    const double rr = q.r[c], uu = q.u[c], vv = q.v[c], ww = q.w[c], ee = q.e[c];
-    const double inv = rcp_nr(rr);
-    const double en = ee * inv - 0.5 * (uu * uu + vv * vv + ww * ww);
-    const double T = ph.cvInv * en;
-    const double pr = rr * ph.Rgas * T;
-    const double hh = (ee + pr) * inv;
-    o.t[c] = (R)T;
-    o.p[c] = (R)pr;
-    o.h[c] = (R)hh;
-    if constexpr (sizeof(R) == 4) {
-        // FP32-RHS mode: transport properties are RHS inputs, evaluated in FP32 from the
-        // FP64 temperature
-        const float Tf = (float)T;
-        const float suth = ph.vexp_is_one ? Tf : powf(Tf, (float)ph.vexp);
-        o.m[c] = suth * (float)ph.invRe;
-        o.l[c] = suth * (float)ph.clam;
-    } else {
-        const double suth = ph.vexp_is_one ? T : pow(T, ph.vexp);
-        o.m[c] = (R)(suth * ph.invRe);
-        o.l[c] = (R)(suth * ph.clam);
-    }
-    if (o.r32) {
-        o.r32[c] = (R)rr; o.u32[c] = (R)uu; o.v32[c] = (R)vv; o.w32[c] = (R)ww;
-    }
-    if (!(T > 0.0) || !(rr > 0.0)) scal[SC_NONFINITE] = 1.0;   // racy flag write, any writer is fine
+    state_point<R>(g, ph, q, o, scal, i, j, k);
 }
 
-// ---------------------------------------------------------------------------------
-// Ghost fill for the stencil inputs rho, u, v, w, T, p, H, mu, lambda.
-//   x: periodic | isothermal wall (BCxNumber1/3: p even, u v w odd, T = 2Tw - T,
-//      mu, lambda, rho, H from the ghost p, T, u, v, w) | boundary layer (bottom: p, T
-//      even, u v w odd, u perturbed; top: linear extrapolation; mu, lambda, rho, H derived)
-//   y: periodic.   z: periodic | linear extrapolation about the end nodes.
-// (src/boundary.h:38-188, src/boundary_condition_x.h:47-115, _y.h:19-58, _z.h:80-332)
-// One thread per ghost cell of the six faces (no edges or corners are ever read).
-// ---------------------------------------------------------------------------------
 template <typename R>
 __global__ void __launch_bounds__(256) k_ghost_state(Geom g, Phys ph, StencilFields<R> f, const double* scal) {
-    const long long G = g.G;
-    const long long nx = 2 * G * g.my * g.mz, ny = 2 * G * g.mx * g.mz, nz = 2 * G * g.mx * g.my;
-    long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    R* F[9] = {f.r, f.u, f.v, f.w, f.t, f.p, f.h, f.m, f.l};
-    if (t < nx) {
-        const int m = (int)(t % G) + 1; t /= G;
-        const int side = (int)(t % 2); t /= 2;
-        const int j = (int)(t % g.my);
-        const int k = (int)(t / g.my);
-        const int ig = side == 0 ? -m : g.mx - 1 + m;
-        const long long cg = g.at(ig, j, k);
-        if (g.xbc == XBC_PER) {
-            const long long cs = g.at(side == 0 ? g.mx - m : m - 1, j, k);
-#pragma unroll
-            for (int q = 0; q < 9; q++) F[q][cg] = F[q][cs];
-            return;
-        }
-        const int ip = side == 0 ? m - 1 : g.mx - m;
-        const long long cp = g.at(ip, j, k);
-        R ug, vg, wg, pg, Tg;
-        if (g.xbc == XBC_WALL) {
-            const double Tw = side == 0 ? ph.twall_bot : ph.twall_top;
-            ug = -f.u[cp]; vg = -f.v[cp]; wg = -f.w[cp];
-            pg = f.p[cp];
-            Tg = (R)(2.0 * Tw) - f.t[cp];
-        } else if (side == 0) {   // boundary layer, wall
-            ug = -f.u[cp]; vg = -f.v[cp]; wg = -f.w[cp];
-            pg = f.p[cp];
-            Tg = f.t[cp];
-            double pv;
-            if (ph.perturbed && wall_perturbation(ph, g.dy, j, k, scal[SC_TIME], &pv)) ug = (R)pv;
-        } else {                  // boundary layer, free stream: extrapolate through the last node
-            const long long cl = g.at(g.mx - 1, j, k);
-            const long long cm = g.at(g.mx - 1 - m, j, k);
-            ug = (R)2.0 * f.u[cl] - f.u[cm];
-            vg = (R)2.0 * f.v[cl] - f.v[cm];
-            wg = (R)2.0 * f.w[cl] - f.w[cm];
-            pg = (R)2.0 * f.p[cl] - f.p[cm];
-            Tg = (R)2.0 * f.t[cl] - f.t[cm];
-        }
-        const R suth = ph.vexp_is_one ? Tg : cns_pow<R>(Tg, (R)ph.vexp);
-        f.u[cg] = ug; f.v[cg] = vg; f.w[cg] = wg; f.p[cg] = pg; f.t[cg] = Tg;
-        f.m[cg] = suth * (R)ph.invRe;
-        f.l[cg] = suth * (R)ph.clam;
-        f.h[cg] = Tg * (R)ph.hcoef + (R)0.5 * (ug * ug + vg * vg + wg * wg);
-        f.r[cg] = pg / ((R)ph.Rgas * Tg);
-        return;
-    }
-    t -= nx;
-    if (t < ny) {
-        const int m = (int)(t % G) + 1; t /= G;
-        const int side = (int)(t % 2); t /= 2;
-        const int i = (int)(t % g.mx);
-        const int k = (int)(t / g.mx);
-        const long long cg = g.at(i, side == 0 ? -m : g.my - 1 + m, k);
-        const long long cs = g.at(i, side == 0 ? g.my - m : m - 1, k);
-#pragma unroll
-        for (int q = 0; q < 9; q++) F[q][cg] = F[q][cs];
-        return;
-    }
-    t -= ny;
-    if (t < nz) {
-        const int m = (int)(t % G) + 1; t /= G;
-        const int side = (int)(t % 2); t /= 2;
-        const int i = (int)(t % g.mx);
-        const int j = (int)(t / g.mx);
-        const long long cg = g.at(i, j, side == 0 ? -m : g.mz - 1 + m);
-        if (!g.zbl) {
-            const long long cs = g.at(i, j, side == 0 ? g.mz - m : m - 1);
-#pragma unroll
-            for (int q = 0; q < 9; q++) F[q][cg] = F[q][cs];
-        } else {
-            const long long c0 = g.at(i, j, side == 0 ? 0 : g.mz - 1);
-            const long long cm = g.at(i, j, side == 0 ? m : g.mz - 1 - m);
-#pragma unroll
-            for (int q = 0; q < 9; q++) F[q][cg] = (R)2.0 * F[q][c0] - F[q][cm];
-        }
-    }
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t < ghost_count(g)) ghost_state_cell<R>(g, ph, f, scal, t);
 }
 
-// ---------------------------------------------------------------------------------
-// Velocity gradients gij[0..8] = d(u,v,w)/d(x,y,z) at the viscous order and the
-// dilatation (derVelX/Y/Z + calcDil, src/calc_stress.cu:20-63,87-96).
-// ---------------------------------------------------------------------------------
 template <typename R, int V>
 __global__ void __launch_bounds__(128) k_grad(Geom g, CoefT<R> cf, const R* __restrict__ u, const R* __restrict__ v,
                                               const R* __restrict__ w, GradOut<R> o) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     const int j = blockIdx.y * blockDim.y + threadIdx.y;
-    const int k = blockIdx.z;
     if (i >= g.mx || j >= g.my) return;
-    const long long c = g.at(i, j, k);
-    const long long st[3] = {1, g.P, g.PS};
-    const R* F[3] = {u, v, w};
-    R out[9];
-#pragma unroll
-    for (int d = 0; d < 3; d++) {
-#pragma unroll
-        for (int q = 0; q < 3; q++) {
-            const R* f = F[q];
-            R s = cf.c1V[d][1] * (__ldg(f + c + st[d]) - __ldg(f + c - st[d]));
-#pragma unroll
-            for (int kk = 2; kk <= V; kk++)
-                s = fma(cf.c1V[d][kk], __ldg(f + c + kk * st[d]) - __ldg(f + c - kk * st[d]), s);
-            if (d == 0 && g.nonuniform_x) s *= cf.xp[i];
-            out[3 * d + q] = s;
-        }
-    }
-#pragma unroll
-    for (int q = 0; q < 9; q++) o.g[q][c] = out[q];
-    o.dil[c] = out[0] + out[4] + out[8];
+    grad_point<R, V>(g, cf, u, v, w, o, i, j, (int)blockIdx.z);
 }
 
-// Dilatation ghosts (BCxNumber2 / BCyNumber1 / BCzNumber1): x periodic | wall: even |
-// boundary layer: bottom even, top extrapolated; y periodic; z periodic | extrapolated.
 template <typename R>
 __global__ void __launch_bounds__(256) k_ghost_scalar(Geom g, R* f) {
-    const long long G = g.G;
-    const long long nx = 2 * G * g.my * g.mz, ny = 2 * G * g.mx * g.mz, nz = 2 * G * g.mx * g.my;
-    long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (t < nx) {
-        const int m = (int)(t % G) + 1; t /= G;
-        const int side = (int)(t % 2); t /= 2;
-        const int j = (int)(t % g.my);
-        const int k = (int)(t / g.my);
-        const long long cg = g.at(side == 0 ? -m : g.mx - 1 + m, j, k);
-        if (g.xbc == XBC_PER) f[cg] = f[g.at(side == 0 ? g.mx - m : m - 1, j, k)];
-        else if (g.xbc == XBC_WALL || side == 0) f[cg] = f[g.at(side == 0 ? m - 1 : g.mx - m, j, k)];
-        else f[cg] = (R)2.0 * f[g.at(g.mx - 1, j, k)] - f[g.at(g.mx - 1 - m, j, k)];
-        return;
-    }
-    t -= nx;
-    if (t < ny) {
-        const int m = (int)(t % G) + 1; t /= G;
-        const int side = (int)(t % 2); t /= 2;
-        const int i = (int)(t % g.mx);
-        const int k = (int)(t / g.mx);
-        f[g.at(i, side == 0 ? -m : g.my - 1 + m, k)] = f[g.at(i, side == 0 ? g.my - m : m - 1, k)];
-        return;
-    }
-    t -= ny;
-    if (t < nz) {
-        const int m = (int)(t % G) + 1; t /= G;
-        const int side = (int)(t % 2); t /= 2;
-        const int i = (int)(t % g.mx);
-        const int j = (int)(t / g.mx);
-        const long long cg = g.at(i, j, side == 0 ? -m : g.mz - 1 + m);
-        if (!g.zbl) f[cg] = f[g.at(i, j, side == 0 ? g.mz - m : m - 1)];
-        else f[cg] = (R)2.0 * f[g.at(i, j, side == 0 ? 0 : g.mz - 1)] - f[g.at(i, j, side == 0 ? m : g.mz - 1 - m)];
-    }
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t < ghost_count(g)) ghost_scalar_cell<R>(g, f, t);
 }
 
 // ---------------------------------------------------------------------------------
@@ -219,7 +44,8 @@ __global__ void __launch_bounds__(256) k_ghost_scalar(Geom g, R* f) {
 //   min dt (deviceCalcDt + minOfThreads, src/calc_stress.cu:140-160, cuda_math.cu:232-259)
 //   sum rho dV, sum rho w dV, sum rhoE dV (integrateThreads, cuda_math.cu:143-171)
 //   sum |u|^2 dV / V (AverageThreads, cuda_math.cu:173-201)
-// partial layout: part[q*RED_BLOCKS + block], q = 0 dt-min, 1 rho, 2 rho w, 3 rhoE, 4 ke
+// partial layout: part[q*RED_BLOCKS + block], q = 0 dt-min, 1 rho, 2 rho w, 3 rhoE,
+// 4 |u|^2, 5 rho |u|^2
 // ---------------------------------------------------------------------------------
 __device__ __forceinline__ double warp_sum(double v) {
 #pragma unroll
@@ -235,9 +61,9 @@ __device__ __forceinline__ double warp_min(double v) {
 template <typename R>
 __global__ void __launch_bounds__(RED_THREADS) k_reduce_partial(Geom g, Phys ph, StateIn q, const R* __restrict__ mu,
                                                                 double* part, int want) {
-    __shared__ double sh[5][RED_THREADS / 32];
+    __shared__ double sh[6][RED_THREADS / 32];
     const long long n = (long long)g.mx * g.my * g.mz;
-    double dtmin = 100000.0, s_r = 0.0, s_rw = 0.0, s_e = 0.0, s_k = 0.0;
+    double dtmin = 100000.0, s_r = 0.0, s_rw = 0.0, s_e = 0.0, s_k = 0.0, s_rk = 0.0;
     for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x) {
         const int i = (int)(t % g.mx);
         const long long jk = t / g.mx;
@@ -258,57 +84,67 @@ __global__ void __launch_bounds__(RED_THREADS) k_reduce_partial(Geom g, Phys ph,
         }
         if (want & RED_FORCE) { s_r += rr * wv; s_rw += rr * ww * wv; }
         if (want & RED_ENERGY) s_e += ee * wv;
-        if (want & RED_KE) s_k += (uu * uu + vv * vv + ww * ww) * wv;
+        if (want & RED_KE) {
+            const double q2 = (uu * uu + vv * vv + ww * ww) * wv;
+            s_k += q2;
+            s_rk += rr * q2;
+        }
     }
-    double vals[5] = {warp_min(dtmin), warp_sum(s_r), warp_sum(s_rw), warp_sum(s_e), warp_sum(s_k)};
+    double vals[6] = {warp_min(dtmin), warp_sum(s_r), warp_sum(s_rw), warp_sum(s_e), warp_sum(s_k), warp_sum(s_rk)};
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
     if (lane == 0)
-        for (int qq = 0; qq < 5; qq++) sh[qq][wid] = vals[qq];
+        for (int qq = 0; qq < 6; qq++) sh[qq][wid] = vals[qq];
     __syncthreads();
     if (threadIdx.x == 0) {
-        double a = sh[0][0], b = 0, c2 = 0, d = 0, e2 = 0;
+        double a = sh[0][0], b = 0, c2 = 0, d = 0, e2 = 0, f2 = 0;
         for (int w = 0; w < RED_THREADS / 32; w++) {
-            a = fmin(a, sh[0][w]); b += sh[1][w]; c2 += sh[2][w]; d += sh[3][w]; e2 += sh[4][w];
+            a = fmin(a, sh[0][w]); b += sh[1][w]; c2 += sh[2][w]; d += sh[3][w]; e2 += sh[4][w]; f2 += sh[5][w];
         }
         part[0 * RED_BLOCKS + blockIdx.x] = a;
         part[1 * RED_BLOCKS + blockIdx.x] = b;
         part[2 * RED_BLOCKS + blockIdx.x] = c2;
         part[3 * RED_BLOCKS + blockIdx.x] = d;
         part[4 * RED_BLOCKS + blockIdx.x] = e2;
+        part[5 * RED_BLOCKS + blockIdx.x] = f2;
     }
 }
 
 // Final pass: one block. Writes dt (and dpdz with forcing, calcPressureGrad law
 // src/calc_stress.cu:16-18) into the scalar block, and the bulk diagnostics into
-// diag[0..1] when requested.
+// diag[2 s], diag[2 s + 1] (s = the device step counter) when requested:
+// unforced: <u.u> (the reference's kin) and <rho |u|^2>/2; forced: bulk velocity
+// int(rho w)/int(rho) and int(rhoE) (calcBulk).
 __global__ void __launch_bounds__(RED_THREADS) k_reduce_final(Phys ph, const double* part, int nblocks, int want,
                                                               double* scal, double* diag) {
-    __shared__ double sh[5][RED_THREADS / 32];
-    double a = 100000.0, b = 0, c = 0, d = 0, e = 0;
+    __shared__ double sh[6][RED_THREADS / 32];
+    double a = 100000.0, b = 0, c = 0, d = 0, e = 0, f = 0;
     for (int t = threadIdx.x; t < nblocks; t += blockDim.x) {
         a = fmin(a, part[0 * RED_BLOCKS + t]);
         b += part[1 * RED_BLOCKS + t];
         c += part[2 * RED_BLOCKS + t];
         d += part[3 * RED_BLOCKS + t];
         e += part[4 * RED_BLOCKS + t];
+        f += part[5 * RED_BLOCKS + t];
     }
-    double vals[5] = {warp_min(a), warp_sum(b), warp_sum(c), warp_sum(d), warp_sum(e)};
+    double vals[6] = {warp_min(a), warp_sum(b), warp_sum(c), warp_sum(d), warp_sum(e), warp_sum(f)};
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
     if (lane == 0)
-        for (int q = 0; q < 5; q++) sh[q][wid] = vals[q];
+        for (int q = 0; q < 6; q++) sh[q][wid] = vals[q];
     __syncthreads();
     if (threadIdx.x != 0) return;
-    a = sh[0][0]; b = c = d = e = 0;
+    a = sh[0][0]; b = c = d = e = f = 0;
     for (int w = 0; w < RED_THREADS / 32; w++) {
-        a = fmin(a, sh[0][w]); b += sh[1][w]; c += sh[2][w]; d += sh[3][w]; e += sh[4][w];
+        a = fmin(a, sh[0][w]); b += sh[1][w]; c += sh[2][w]; d += sh[3][w]; e += sh[4][w]; f += sh[5][w];
     }
     if (want & RED_DT) {
         scal[SC_DT] = a;
         if (want & RED_FORCE) scal[SC_DPDZ] = 0.99 * scal[SC_DPDZ] - 0.5 * (c / b - 1);
     }
     if (diag) {
-        if (want & RED_KE) { diag[0] = e / ph.Lx / ph.Ly / ph.Lz; diag[1] = __longlong_as_double(0x7ff8000000000000LL); }
-        else if (want & RED_FORCE) { diag[0] = c / b; diag[1] = d; }
+        double* dg = diag + 2 * (long long)scal[SC_STEP];
+        const double vol = ph.Lx * ph.Ly * ph.Lz;
+        if (want & RED_KE) { dg[0] = e / ph.Lx / ph.Ly / ph.Lz; dg[1] = 0.5 * f / vol; }
+        else if (want & RED_FORCE) { dg[0] = c / b; dg[1] = d; }
     }
 }
 
@@ -339,10 +175,7 @@ __global__ void __launch_bounds__(256) k_pack(Geom g, const T* __restrict__ src,
 // ---------------------------------------------------------------------------------
 static inline dim3 point_grid(const Geom& g) { return dim3((g.mx + 31) / 32, (g.my + 3) / 4, g.mz); }
 static inline dim3 point_block() { return dim3(32, 4, 1); }
-static inline unsigned ghost_blocks(const Geom& g) {
-    long long n = 2LL * g.G * ((long long)g.my * g.mz + (long long)g.mx * g.mz + (long long)g.mx * g.my);
-    return (unsigned)((n + 255) / 256);
-}
+static inline unsigned ghost_blocks(const Geom& g) { return (unsigned)((ghost_count(g) + 255) / 256); }
 
 template <typename R>
 void launch_state(const Geom& g, const Phys& ph, const StateIn& q, const DerivedOut<R>& o, double* scal,

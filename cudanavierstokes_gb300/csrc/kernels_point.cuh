@@ -1,0 +1,220 @@
+// kernels_point.cuh -- per-point / per-ghost-cell bodies of the stage phases, shared by
+// the single-solver kernels (kernels_common.cu) and the batched persistent stage kernel
+// (batch.cu).
+#pragma once
+#include "cns_common.cuh"
+#include "cns_internal.h"
+
+namespace cns {
+
+// ---------------------------------------------------------------------------------
+// State recovery (calcState, src/cuda_main.cu:218-242): T, p, H, mu, lambda from
+// rho, u, v, w, rhoE in FP64; stored as R. In FP32-RHS mode the FP32 stencil copies of
+// rho, u, v, w are written too and mu, lambda are evaluated in FP32 from the FP64 T.
+// ---------------------------------------------------------------------------------
+template <typename R>
+__device__ __forceinline__ void state_point(const Geom& g, const Phys& ph, const StateIn& q, const DerivedOut<R>& o,
+                                            double* scal, int i, int j, int k) {
+    const long long c = g.at(i, j, k);
+    const double rr = q.r[c], uu = q.u[c], vv = q.v[c], ww = q.w[c], ee = q.e[c];
+    const double inv = rcp_nr(rr);
+    const double en = ee * inv - 0.5 * (uu * uu + vv * vv + ww * ww);
+    const double T = ph.cvInv * en;
+    const double pr = rr * ph.Rgas * T;
+    const double hh = (ee + pr) * inv;
+    o.t[c] = (R)T;
+    o.p[c] = (R)pr;
+    o.h[c] = (R)hh;
+    if constexpr (sizeof(R) == 4) {
+        const float Tf = (float)T;
+        const float suth = ph.vexp_is_one ? Tf : powf(Tf, (float)ph.vexp);
+        o.m[c] = suth * (float)ph.invRe;
+        o.l[c] = suth * (float)ph.clam;
+    } else {
+        const double suth = ph.vexp_is_one ? T : pow(T, ph.vexp);
+        o.m[c] = (R)(suth * ph.invRe);
+        o.l[c] = (R)(suth * ph.clam);
+    }
+    if (o.r32) {
+        o.r32[c] = (R)rr; o.u32[c] = (R)uu; o.v32[c] = (R)vv; o.w32[c] = (R)ww;
+    }
+    if (!(T > 0.0) || !(rr > 0.0)) scal[SC_NONFINITE] = 1.0;   // racy flag write, any writer is fine
+}
+
+// Stage 0 of a step advances the simulation time by dt (deviceAdvanceTime) and, with a
+// time log, stores the new time at the device step counter and advances the counter.
+__device__ __forceinline__ void advance_time(double* scal, double* time_log) {
+    const double tn = scal[SC_TIME] + scal[SC_DT];
+    scal[SC_TIME] = tn;
+    if (time_log) {
+        const long long st = (long long)scal[SC_STEP];
+        time_log[st] = tn;
+        scal[SC_STEP] = (double)(st + 1);
+    }
+}
+
+__host__ __device__ __forceinline__ long long ghost_count(const Geom& g) {
+    const long long G = g.G;
+    return 2 * G * ((long long)g.my * g.mz + (long long)g.mx * g.mz + (long long)g.mx * g.my);
+}
+
+// ---------------------------------------------------------------------------------
+// Ghost cell t of the stencil inputs rho, u, v, w, T, p, H, mu, lambda.
+//   x: periodic | isothermal wall (BCxNumber1/3: p even, u v w odd, T = 2Tw - T,
+//      mu, lambda, rho, H from the ghost p, T, u, v, w) | boundary layer (bottom: p, T
+//      even, u v w odd, u perturbed; top: linear extrapolation; mu, lambda, rho, H derived)
+//   y: periodic.   z: periodic | linear extrapolation about the end nodes.
+// (src/boundary.h:38-188, src/boundary_condition_x.h:47-115, _y.h:19-58, _z.h:80-332)
+// Only the six faces are filled (no stencil reads an edge or a corner).
+// ---------------------------------------------------------------------------------
+template <typename R>
+__device__ __forceinline__ void ghost_state_cell(const Geom& g, const Phys& ph, const StencilFields<R>& f,
+                                                 const double* scal, long long t) {
+    const long long G = g.G;
+    const long long nx = 2 * G * g.my * g.mz, ny = 2 * G * g.mx * g.mz, nz = 2 * G * g.mx * g.my;
+    R* F[9] = {f.r, f.u, f.v, f.w, f.t, f.p, f.h, f.m, f.l};
+    if (t < nx) {
+        const int m = (int)(t % G) + 1; t /= G;
+        const int side = (int)(t % 2); t /= 2;
+        const int j = (int)(t % g.my);
+        const int k = (int)(t / g.my);
+        const int ig = side == 0 ? -m : g.mx - 1 + m;
+        const long long cg = g.at(ig, j, k);
+        if (g.xbc == XBC_PER) {
+            const long long cs = g.at(side == 0 ? g.mx - m : m - 1, j, k);
+#pragma unroll
+            for (int q = 0; q < 9; q++) F[q][cg] = F[q][cs];
+            return;
+        }
+        const int ip = side == 0 ? m - 1 : g.mx - m;
+        const long long cp = g.at(ip, j, k);
+        R ug, vg, wg, pg, Tg;
+        if (g.xbc == XBC_WALL) {
+            const double Tw = side == 0 ? ph.twall_bot : ph.twall_top;
+            ug = -f.u[cp]; vg = -f.v[cp]; wg = -f.w[cp];
+            pg = f.p[cp];
+            Tg = (R)(2.0 * Tw) - f.t[cp];
+        } else if (side == 0) {   // boundary layer, wall
+            ug = -f.u[cp]; vg = -f.v[cp]; wg = -f.w[cp];
+            pg = f.p[cp];
+            Tg = f.t[cp];
+            double pv;
+            if (ph.perturbed && wall_perturbation(ph, g.dy, j, k, scal[SC_TIME], &pv)) ug = (R)pv;
+        } else {                  // boundary layer, free stream: extrapolate through the last node
+            const long long cl = g.at(g.mx - 1, j, k);
+            const long long cm = g.at(g.mx - 1 - m, j, k);
+            ug = (R)2.0 * f.u[cl] - f.u[cm];
+            vg = (R)2.0 * f.v[cl] - f.v[cm];
+            wg = (R)2.0 * f.w[cl] - f.w[cm];
+            pg = (R)2.0 * f.p[cl] - f.p[cm];
+            Tg = (R)2.0 * f.t[cl] - f.t[cm];
+        }
+        const R suth = ph.vexp_is_one ? Tg : cns_pow<R>(Tg, (R)ph.vexp);
+        f.u[cg] = ug; f.v[cg] = vg; f.w[cg] = wg; f.p[cg] = pg; f.t[cg] = Tg;
+        f.m[cg] = suth * (R)ph.invRe;
+        f.l[cg] = suth * (R)ph.clam;
+        f.h[cg] = Tg * (R)ph.hcoef + (R)0.5 * (ug * ug + vg * vg + wg * wg);
+        f.r[cg] = pg / ((R)ph.Rgas * Tg);
+        return;
+    }
+    t -= nx;
+    if (t < ny) {
+        const int m = (int)(t % G) + 1; t /= G;
+        const int side = (int)(t % 2); t /= 2;
+        const int i = (int)(t % g.mx);
+        const int k = (int)(t / g.mx);
+        const long long cg = g.at(i, side == 0 ? -m : g.my - 1 + m, k);
+        const long long cs = g.at(i, side == 0 ? g.my - m : m - 1, k);
+#pragma unroll
+        for (int q = 0; q < 9; q++) F[q][cg] = F[q][cs];
+        return;
+    }
+    t -= ny;
+    if (t < nz) {
+        const int m = (int)(t % G) + 1; t /= G;
+        const int side = (int)(t % 2); t /= 2;
+        const int i = (int)(t % g.mx);
+        const int j = (int)(t / g.mx);
+        const long long cg = g.at(i, j, side == 0 ? -m : g.mz - 1 + m);
+        if (!g.zbl) {
+            const long long cs = g.at(i, j, side == 0 ? g.mz - m : m - 1);
+#pragma unroll
+            for (int q = 0; q < 9; q++) F[q][cg] = F[q][cs];
+        } else {
+            const long long c0 = g.at(i, j, side == 0 ? 0 : g.mz - 1);
+            const long long cm = g.at(i, j, side == 0 ? m : g.mz - 1 - m);
+#pragma unroll
+            for (int q = 0; q < 9; q++) F[q][cg] = (R)2.0 * F[q][c0] - F[q][cm];
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------------
+// Velocity gradients gij[0..8] = d(u,v,w)/d(x,y,z) at the viscous order and the
+// dilatation (derVelX/Y/Z + calcDil, src/calc_stress.cu:20-63,87-96).
+// ---------------------------------------------------------------------------------
+template <typename R, int V>
+__device__ __forceinline__ void grad_point(const Geom& g, const CoefT<R>& cf, const R* __restrict__ u,
+                                           const R* __restrict__ v, const R* __restrict__ w, const GradOut<R>& o,
+                                           int i, int j, int k) {
+    const long long c = g.at(i, j, k);
+    const long long st[3] = {1, g.P, g.PS};
+    const R* F[3] = {u, v, w};
+    R out[9];
+#pragma unroll
+    for (int d = 0; d < 3; d++) {
+#pragma unroll
+        for (int q = 0; q < 3; q++) {
+            const R* f = F[q];
+            R s = cf.c1V[d][1] * (__ldg(f + c + st[d]) - __ldg(f + c - st[d]));
+#pragma unroll
+            for (int kk = 2; kk <= V; kk++)
+                s = fma(cf.c1V[d][kk], __ldg(f + c + kk * st[d]) - __ldg(f + c - kk * st[d]), s);
+            if (d == 0 && g.nonuniform_x) s *= cf.xp[i];
+            out[3 * d + q] = s;
+        }
+    }
+#pragma unroll
+    for (int q = 0; q < 9; q++) o.g[q][c] = out[q];
+    o.dil[c] = out[0] + out[4] + out[8];
+}
+
+// Dilatation ghost cell t (BCxNumber2 / BCyNumber1 / BCzNumber1): x periodic | wall:
+// even | boundary layer: bottom even, top extrapolated; y periodic; z periodic | extrapolated.
+template <typename R>
+__device__ __forceinline__ void ghost_scalar_cell(const Geom& g, R* f, long long t) {
+    const long long G = g.G;
+    const long long nx = 2 * G * g.my * g.mz, ny = 2 * G * g.mx * g.mz, nz = 2 * G * g.mx * g.my;
+    if (t < nx) {
+        const int m = (int)(t % G) + 1; t /= G;
+        const int side = (int)(t % 2); t /= 2;
+        const int j = (int)(t % g.my);
+        const int k = (int)(t / g.my);
+        const long long cg = g.at(side == 0 ? -m : g.mx - 1 + m, j, k);
+        if (g.xbc == XBC_PER) f[cg] = f[g.at(side == 0 ? g.mx - m : m - 1, j, k)];
+        else if (g.xbc == XBC_WALL || side == 0) f[cg] = f[g.at(side == 0 ? m - 1 : g.mx - m, j, k)];
+        else f[cg] = (R)2.0 * f[g.at(g.mx - 1, j, k)] - f[g.at(g.mx - 1 - m, j, k)];
+        return;
+    }
+    t -= nx;
+    if (t < ny) {
+        const int m = (int)(t % G) + 1; t /= G;
+        const int side = (int)(t % 2); t /= 2;
+        const int i = (int)(t % g.mx);
+        const int k = (int)(t / g.mx);
+        f[g.at(i, side == 0 ? -m : g.my - 1 + m, k)] = f[g.at(i, side == 0 ? g.my - m : m - 1, k)];
+        return;
+    }
+    t -= ny;
+    if (t < nz) {
+        const int m = (int)(t % G) + 1; t /= G;
+        const int side = (int)(t % 2); t /= 2;
+        const int i = (int)(t % g.mx);
+        const int j = (int)(t / g.mx);
+        const long long cg = g.at(i, j, side == 0 ? -m : g.mz - 1 + m);
+        if (!g.zbl) f[cg] = f[g.at(i, j, side == 0 ? g.mz - m : m - 1)];
+        else f[cg] = (R)2.0 * f[g.at(i, j, side == 0 ? 0 : g.mz - 1)] - f[g.at(i, j, side == 0 ? m : g.mz - 1 - m)];
+    }
+}
+
+}  // namespace cns

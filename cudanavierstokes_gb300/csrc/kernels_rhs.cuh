@@ -142,13 +142,10 @@ __device__ __forceinline__ void rhs_direction(const Geom& g, const CoefT<R>& cf,
     acc[1 + DIR] -= dp;
 }
 
+// RHS + stage update of one interior point (i, j, k)
 template <typename R, int S, int V>
-__global__ void __launch_bounds__(128) k_rhs(Geom g, CoefT<R> cf, RhsIn<R> in, Update<R> up,
-                                             const double* __restrict__ scal, int quirk) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    const int j = blockIdx.y * blockDim.y + threadIdx.y;
-    const int k = blockIdx.z;
-    if (i >= g.mx || j >= g.my) return;
+__device__ __forceinline__ void rhs_point(const Geom& g, const CoefT<R>& cf, const RhsIn<R>& in, const Update<R>& up,
+                                          const double* __restrict__ scal, int quirk, int i, int j, int k) {
     const long long c = g.at(i, j, k);
 
     R Gr[9];
@@ -168,43 +165,53 @@ __global__ void __launch_bounds__(128) k_rhs(Geom g, CoefT<R> cf, RhsIn<R> in, U
     acc[3] += W[2];
     acc[4] += fma(m0, diss, cond) + fma(u0, W[0], fma(v0, W[1], w0 * W[2]));
 
-    // ---- FP64 from here: body force, sponge, stage update ----
-    const double dpdz = scal[SC_DPDZ];
+    // ---- body force and sponge (RHS terms, arithmetic type R) ----
+    const R dpdz = (R)scal[SC_DPDZ];
+    acc[3] += dpdz;
+    acc[4] = fma(dpdz, w0, acc[4]);
     const double rr = up.qin.r[c], uu = up.qin.u[c], vv = up.qin.v[c], ww = up.qin.w[c], ee = up.qin.e[c];
-    double Rd[5] = {(double)acc[0], (double)acc[1], (double)acc[2], (double)acc[3], (double)acc[4]};
-    Rd[3] += dpdz;
-    Rd[4] += dpdz * (double)w0;
     if (up.spx) {
-        const double s = up.spx[i] + up.spz[k];
+        const R sg = (R)(up.spx[i] + up.spz[k]);
         const long long i2 = (long long)i + (long long)k * g.mx;
-        Rd[0] += s * (up.rref[i2] - rr);
-        Rd[1] += s * (up.uref[i2] - rr * uu);
-        Rd[2] += s * (up.vref[i2] - rr * vv);
-        Rd[3] += s * (up.wref[i2] - rr * ww);
-        Rd[4] += s * (up.eref[i2] - ee);
+        if constexpr (sizeof(R) == 8) {
+            acc[0] += sg * (up.rref[i2] - rr);
+            acc[1] += sg * (up.uref[i2] - rr * uu);
+            acc[2] += sg * (up.vref[i2] - rr * vv);
+            acc[3] += sg * (up.wref[i2] - rr * ww);
+            acc[4] += sg * (up.eref[i2] - ee);
+        } else {
+            acc[0] += sg * ((R)up.rref[i2] - r0);
+            acc[1] += sg * ((R)up.uref[i2] - r0 * u0);
+            acc[2] += sg * ((R)up.vref[i2] - r0 * v0);
+            acc[3] += sg * ((R)up.wref[i2] - r0 * w0);
+            acc[4] += sg * ((R)up.eref[i2] - (R)ee);
+        }
     }
     if (up.kind == ST_RHS_ONLY) {
 #pragma unroll
-        for (int q = 0; q < 5; q++) up.rb[q][c] = (R)Rd[q];
+        for (int q = 0; q < 5; q++) up.rb[q][c] = acc[q];
         return;
     }
+    // ---- stage update: the RHS combination in R, the accumulation into the state in FP64 ----
     const double dt = scal[SC_DT];
     double qn[5];
     if (up.kind == ST_LS) {
         const double q0[5] = {rr, uu * rr, vv * rr, ww * rr, ee};
+        const R a = (R)up.a, b = (R)up.b;
 #pragma unroll
         for (int q = 0; q < 5; q++) {
-            const double x = up.a != 0.0 ? up.a * (double)up.rb[q][c] + up.b * Rd[q] : up.b * Rd[q];
-            qn[q] = q0[q] + dt * x;
-            up.rb[q][c] = (R)Rd[q];
+            const R x = up.a != 0.0 ? fma(a, up.rb[q][c], b * acc[q]) : b * acc[q];
+            qn[q] = fma(dt, (double)x, q0[q]);
+            up.rb[q][c] = acc[q];
         }
     } else if (up.kind == ST_C1 || up.kind == ST_R4_1) {
         const double q0[5] = {rr, rr * uu, rr * vv, rr * ww, ee};
 #pragma unroll
         for (int q = 0; q < 5; q++) {
             up.q0[q][c] = q0[q];
-            if (up.kind == ST_C1) { qn[q] = q0[q] + Rd[q] * dt / 2.0; up.rb[q][c] = (R)Rd[q]; }
-            else { qn[q] = q0[q] + 0.5 * dt * Rd[q]; up.k2[q][c] = (R)Rd[q]; }
+            const double Rd = (double)acc[q];
+            if (up.kind == ST_C1) { qn[q] = q0[q] + Rd * dt / 2.0; up.rb[q][c] = acc[q]; }
+            else { qn[q] = q0[q] + 0.5 * dt * Rd; up.k2[q][c] = acc[q]; }
         }
     } else {
         double q0[5];
@@ -212,12 +219,13 @@ __global__ void __launch_bounds__(128) k_rhs(Geom g, CoefT<R> cf, RhsIn<R> in, U
         for (int q = 0; q < 5; q++) q0[q] = up.q0[q][c];
 #pragma unroll
         for (int q = 0; q < 5; q++) {
+            const double Rd = (double)acc[q];
             switch (up.kind) {
-            case ST_C2: qn[q] = q0[q] + (2 * Rd[q] - (double)up.rb[q][c]) * dt; up.k2[q][c] = (R)Rd[q]; break;
-            case ST_C3: qn[q] = q0[q] + dt * ((double)up.rb[q][c] + 4 * (double)up.k2[q][c] + Rd[q]) / 6.; break;
-            case ST_R4_2: up.k2[q][c] = (R)((double)up.k2[q][c] + 2.0 * Rd[q]); qn[q] = q0[q] + 0.5 * dt * Rd[q]; break;
-            case ST_R4_3: up.k2[q][c] = (R)((double)up.k2[q][c] + 2.0 * Rd[q]); qn[q] = q0[q] + dt * Rd[q]; break;
-            default: qn[q] = q0[q] + dt / 6.0 * ((double)up.k2[q][c] + Rd[q]); break;
+            case ST_C2: qn[q] = q0[q] + (2 * Rd - (double)up.rb[q][c]) * dt; up.k2[q][c] = acc[q]; break;
+            case ST_C3: qn[q] = q0[q] + dt * ((double)up.rb[q][c] + 4 * (double)up.k2[q][c] + Rd) / 6.; break;
+            case ST_R4_2: up.k2[q][c] = (R)((double)up.k2[q][c] + 2.0 * Rd); qn[q] = q0[q] + 0.5 * dt * Rd; break;
+            case ST_R4_3: up.k2[q][c] = (R)((double)up.k2[q][c] + 2.0 * Rd); qn[q] = q0[q] + dt * Rd; break;
+            default: qn[q] = q0[q] + dt / 6.0 * ((double)up.k2[q][c] + Rd); break;
             }
         }
     }
@@ -227,6 +235,15 @@ __global__ void __launch_bounds__(128) k_rhs(Geom g, CoefT<R> cf, RhsIn<R> in, U
     up.qout.v[c] = qn[2] * inv;
     up.qout.w[c] = qn[3] * inv;
     up.qout.e[c] = qn[4];
+}
+
+template <typename R, int S, int V>
+__global__ void __launch_bounds__(128) k_rhs(Geom g, CoefT<R> cf, RhsIn<R> in, Update<R> up,
+                                             const double* __restrict__ scal, int quirk) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y;
+    if (i >= g.mx || j >= g.my) return;
+    rhs_point<R, S, V>(g, cf, in, up, scal, quirk, i, j, (int)blockIdx.z);
 }
 
 template <typename R>

@@ -21,6 +21,7 @@
 #include "../../include/cns.h"
 #include "cns_internal.h"
 #include "grid.h"
+#include "solver_internal.h"
 
 using namespace cns;
 
@@ -63,79 +64,6 @@ int set_error(int code, const char* msg) {
     return code;
 }
 }  // namespace cns
-
-struct cns_solver {
-    cns_params p{};
-    int device = 0;
-    cudaStream_t stream = nullptr, own_stream = nullptr;
-    HostGrid hg;
-    Geom geom{};
-    Phys phys{};
-    CoefT<double> cf64{};
-    CoefT<float> cf32{};
-    bool fp32 = false;
-    size_t rsz = 8;              // bytes of the RHS arithmetic type
-    long long nalloc = 0;        // elements of one padded field
-    std::vector<void*> allocs;
-    int64_t bytes = 0;
-    int64_t launches = 0;
-
-    double* q[2][5] = {};        // state ping-pong (rho, u, v, w, rhoE)
-    int cur = 0;
-    void* der[5] = {};           // h, t, p, mu, lambda   (R)
-    void* s32[4] = {};           // FP32 stencil copies of rho, u, v, w
-    void* dil = nullptr;         // (R)
-    void* grad[9] = {};          // (R)
-    void* rb[5] = {};            // RHS register (R)
-    void* k2[5] = {};            // classic RK3 k2 / RK4 accumulator (R)
-    double* q0[5] = {};          // classic schemes: conserved state at the step start
-    double* staging = nullptr;   // N doubles, host <-> device layout conversion
-    double* scal = nullptr;      // device scalars (SC_*)
-    double* part = nullptr;      // reduction partials 5 * RED_BLOCKS
-    double* diag = nullptr;      // per-step bulk diagnostics (2 per step)
-    double* tlog = nullptr;      // per-step time
-    int diag_cap = 0;
-    double *xp_d = nullptr, *cvsx_d = nullptr, *wvol_d = nullptr, *dxv_d = nullptr;
-    float *xp_f = nullptr, *cvsx_f = nullptr;
-    double *spx = nullptr, *spz = nullptr, *rref = nullptr, *uref = nullptr, *vref = nullptr, *wref = nullptr,
-           *eref = nullptr;
-    bool has_sponge = false;
-    bool initialized = false;
-
-    template <typename T>
-    int alloc(T** ptr, size_t n) {
-        void* p0 = nullptr;
-        cudaError_t e = cudaMalloc(&p0, n * sizeof(T));
-        if (e != cudaSuccess) {
-            cudaGetLastError();
-            return fail(CNS_ERR_OOM, "cudaMalloc of %zu bytes failed: %s", n * sizeof(T), cudaGetErrorString(e));
-        }
-        allocs.push_back(p0);
-        bytes += (int64_t)(n * sizeof(T));
-        *ptr = (T*)p0;
-        return CNS_OK;
-    }
-    int alloc_field(void** ptr, size_t esz) {
-        void* p0 = nullptr;
-        cudaError_t e = cudaMalloc(&p0, (size_t)nalloc * esz);
-        if (e != cudaSuccess) {
-            cudaGetLastError();
-            return fail(CNS_ERR_OOM, "cudaMalloc of a %lld-element field failed: %s", nalloc, cudaGetErrorString(e));
-        }
-        allocs.push_back(p0);
-        bytes += (int64_t)((size_t)nalloc * esz);
-        *ptr = p0;
-        return CNS_OK;
-    }
-    ~cns_solver() {
-        int prev = -1;
-        cudaGetDevice(&prev);
-        cudaSetDevice(device);
-        for (void* a : allocs) cudaFree(a);
-        if (own_stream) cudaStreamDestroy(own_stream);
-        if (prev >= 0) cudaSetDevice(prev);
-    }
-};
 
 namespace {
 
@@ -262,7 +190,9 @@ int rhs_any(cns_solver* h, int kind, double a, double b) {
     return h->fp32 ? rhs_phase<float>(h, kind, a, b) : rhs_phase<double>(h, kind, a, b);
 }
 
-int reduce_any(cns_solver* h, int want, double* diag) {
+}  // namespace
+
+int cns::solver_reduce(cns_solver* h, int want, double* diag) {
     if (h->fp32) launch_reduce<float>(h->geom, h->phys, state_in(h, h->cur), (const float*)h->der[3], h->part, want,
                                       h->scal, diag, h->stream);
     else launch_reduce<double>(h->geom, h->phys, state_in(h, h->cur), (const double*)h->der[3], h->part, want,
@@ -271,6 +201,8 @@ int reduce_any(cns_solver* h, int want, double* diag) {
     CKL();
     return CNS_OK;
 }
+
+namespace {
 
 const double WRAY_A[3] = {0., -17. / 60., -5. / 12.};   // src/cuda_main.cu:10-11
 const double WRAY_B[3] = {8. / 15., 5. / 12., 3. / 4.};
@@ -290,6 +222,34 @@ int step_stages(cns_solver* h, double* time_log) {
         else kind = ST_R4_1 + s;
         if ((rc = rhs_any(h, kind, a, b))) return rc;
     }
+    return CNS_OK;
+}
+
+// one time step through the captured graph of the current parity (captured on first use)
+int step_graph(cns_solver* h) {
+    const int c = h->cur;
+    const int nst = h->p.scheme == CNS_RK4_CLASSIC ? 4 : 3;
+    if (!h->step_exec[c]) {
+        const int64_t l0 = h->launches;
+        CK(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
+        int rc = step_stages(h, h->tlog);
+        cudaGraph_t graph = nullptr;
+        cudaError_t e = cudaStreamEndCapture(h->stream, &graph);
+        h->cur = c;
+        h->step_kernels = h->launches - l0;
+        h->launches = l0;
+        if (rc) {
+            if (graph) cudaGraphDestroy(graph);
+            return rc;
+        }
+        CK(e);
+        e = cudaGraphInstantiate(&h->step_exec[c], graph, 0);
+        cudaGraphDestroy(graph);
+        CK(e);
+    }
+    CK(cudaGraphLaunch(h->step_exec[c], h->stream));
+    h->launches += h->step_kernels;
+    h->cur = c ^ (nst & 1);
     return CNS_OK;
 }
 
@@ -443,7 +403,7 @@ int cns_create(const cns_params* pin, int device, cns_solver** out) {
     }
     if (!rc) rc = h->alloc(&h->staging, N);
     if (!rc) rc = h->alloc(&h->scal, SC_COUNT);
-    if (!rc) rc = h->alloc(&h->part, 5 * RED_BLOCKS);
+    if (!rc) rc = h->alloc(&h->part, 6 * RED_BLOCKS);
     if (!rc) rc = upload_grid_tables(h);
     if (rc) { delete h; return rc; }
     h->cf64.xp = h->xp_d; h->cf64.cvsx = h->cvsx_d;
@@ -509,6 +469,7 @@ int cns_set_sponge(cns_solver* h, const double* sx, const double* sz, const doub
     CK(cudaMemcpy(h->wref, wm.data(), n2 * 8, cudaMemcpyHostToDevice));
     CK(cudaMemcpy(h->eref, er, n2 * 8, cudaMemcpyHostToDevice));
     h->has_sponge = h->p.boundary_layer != 0;
+    h->drop_graphs();
     return CNS_OK;
 }
 
@@ -592,11 +553,15 @@ int cns_run(cns_solver* h, int nsteps, double* par1, double* par2, double* time)
     CK(cudaSetDevice(h->device));
     int rc;
     if (h->diag_cap < nsteps) {
-        // grow the per-step log buffers (allocation stays with the handle)
+        // grow the per-step log buffers (allocation stays with the handle; captured step
+        // graphs refer to the old buffers and are dropped)
         double *d = nullptr, *t = nullptr;
-        if ((rc = h->alloc(&d, 2 * (size_t)nsteps)) || (rc = h->alloc(&t, (size_t)nsteps))) return rc;
-        h->diag = d; h->tlog = t; h->diag_cap = nsteps;
+        const int cap = nsteps < 1024 ? 1024 : nsteps;
+        if ((rc = h->alloc(&d, 2 * (size_t)cap)) || (rc = h->alloc(&t, (size_t)cap))) return rc;
+        h->diag = d; h->tlog = t; h->diag_cap = cap;
+        h->drop_graphs();
     }
+    CK(cudaMemsetAsync(h->scal + SC_STEP, 0, sizeof(double), h->stream));   // step counter of this run
     const int forcing = h->p.forcing != 0;
     for (int s = 0; s < nsteps; s++) {
         int want = 0;
@@ -604,10 +569,11 @@ int cns_run(cns_solver* h, int nsteps, double* par1, double* par2, double* time)
         if (s % h->p.check_cfl == 0) want |= RED_DT | (forcing ? RED_FORCE : 0);
         if (s % h->p.check_bulk == 0) {
             want |= forcing ? (RED_FORCE | RED_ENERGY) : RED_KE;
-            dg = h->diag + 2 * (size_t)s;
+            dg = h->diag;
         }
-        if (want && (rc = reduce_any(h, want, dg))) return rc;
-        if ((rc = step_stages(h, h->tlog + s))) return rc;
+        if (want && (rc = cns::solver_reduce(h, want, dg))) return rc;
+        rc = h->use_graphs ? step_graph(h) : step_stages(h, h->tlog);
+        if (rc) return rc;
     }
     rc = sync_and_check(h);
     if (rc) return rc;
@@ -621,6 +587,13 @@ int cns_run(cns_solver* h, int nsteps, double* par1, double* par2, double* time)
         }
     }
     if (time) CK(cudaMemcpy(time, h->tlog, (size_t)nsteps * 8, cudaMemcpyDeviceToHost));
+    return CNS_OK;
+}
+
+int cns_set_graphs(cns_solver* h, int enable) {
+    if (!h) return fail(CNS_ERR_INVALID, "handle is NULL");
+    h->use_graphs = enable != 0;
+    if (!h->use_graphs) h->drop_graphs();
     return CNS_OK;
 }
 

@@ -1,0 +1,118 @@
+// solver_internal.h -- the solver handle (internal; shared by solver.cu and batch.cu).
+#pragma once
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <vector>
+
+#include "../../include/cns.h"
+#include "cns_internal.h"
+#include "grid.h"
+
+namespace cns {
+int set_error(int code, const char* msg);
+}
+
+struct cns_solver {
+    using HostGrid = cns::HostGrid;
+    using Geom = cns::Geom;
+    using Phys = cns::Phys;
+    template <typename R> using CoefT = cns::CoefT<R>;
+    cns_params p{};
+    int device = 0;
+    cudaStream_t stream = nullptr, own_stream = nullptr;
+    HostGrid hg;
+    Geom geom{};
+    Phys phys{};
+    CoefT<double> cf64{};
+    CoefT<float> cf32{};
+    bool fp32 = false;
+    size_t rsz = 8;              // bytes of the RHS arithmetic type
+    long long nalloc = 0;        // elements of one padded field
+    std::vector<void*> allocs;
+    int64_t bytes = 0;
+    int64_t launches = 0;
+
+    double* q[2][5] = {};        // state ping-pong (rho, u, v, w, rhoE)
+    int cur = 0;
+    void* der[5] = {};           // h, t, p, mu, lambda   (R)
+    void* s32[4] = {};           // FP32 stencil copies of rho, u, v, w
+    void* dil = nullptr;         // (R)
+    void* grad[9] = {};          // (R)
+    void* rb[5] = {};            // RHS register (R)
+    void* k2[5] = {};            // classic RK3 k2 / RK4 accumulator (R)
+    double* q0[5] = {};          // classic schemes: conserved state at the step start
+    double* staging = nullptr;   // N doubles, host <-> device layout conversion
+    double* scal = nullptr;      // device scalars (SC_*)
+    double* part = nullptr;      // reduction partials 5 * RED_BLOCKS
+    double* diag = nullptr;      // per-step bulk diagnostics (2 per step)
+    double* tlog = nullptr;      // per-step time
+    int diag_cap = 0;
+    double *xp_d = nullptr, *cvsx_d = nullptr, *wvol_d = nullptr, *dxv_d = nullptr;
+    float *xp_f = nullptr, *cvsx_f = nullptr;
+    double *spx = nullptr, *spz = nullptr, *rref = nullptr, *uref = nullptr, *vref = nullptr, *wref = nullptr,
+           *eref = nullptr;
+    bool has_sponge = false;
+    bool initialized = false;
+    // one captured time step per starting ping-pong parity (kernel arguments are
+    // step-invariant: per-step log slots come from the device step counter)
+    cudaGraphExec_t step_exec[2] = {nullptr, nullptr};
+    int64_t step_kernels = 0;
+    bool use_graphs = true;
+
+    void drop_graphs() {
+        for (int c = 0; c < 2; c++)
+            if (step_exec[c]) { cudaGraphExecDestroy(step_exec[c]); step_exec[c] = nullptr; }
+    }
+
+    template <typename T>
+    int alloc(T** ptr, size_t n) {
+        void* p0 = nullptr;
+        cudaError_t e = cudaMalloc(&p0, n * sizeof(T));
+        if (e != cudaSuccess) {
+            cudaGetLastError();
+            return cns::set_error(CNS_ERR_OOM, "cudaMalloc failed");
+        }
+        allocs.push_back(p0);
+        bytes += (int64_t)(n * sizeof(T));
+        *ptr = (T*)p0;
+        return CNS_OK;
+    }
+    int alloc_field(void** ptr, size_t esz) {
+        void* p0 = nullptr;
+        cudaError_t e = cudaMalloc(&p0, (size_t)nalloc * esz);
+        if (e != cudaSuccess) {
+            cudaGetLastError();
+            return cns::set_error(CNS_ERR_OOM, "cudaMalloc of a field failed");
+        }
+        allocs.push_back(p0);
+        bytes += (int64_t)((size_t)nalloc * esz);
+        *ptr = p0;
+        return CNS_OK;
+    }
+    ~cns_solver() {
+        int prev = -1;
+        cudaGetDevice(&prev);
+        cudaSetDevice(device);
+        drop_graphs();
+        for (void* a : allocs) cudaFree(a);
+        if (own_stream) cudaStreamDestroy(own_stream);
+        if (prev >= 0) cudaSetDevice(prev);
+    }
+};
+
+
+namespace cns {
+// parity swap: make buffer `want` the current state buffer (pointer swap, no copy)
+inline void solver_set_parity(cns_solver* h, int want) {
+    if (h->cur == want) return;
+    for (int f = 0; f < 5; f++) {
+        double* t = h->q[0][f];
+        h->q[0][f] = h->q[1][f];
+        h->q[1][f] = t;
+    }
+    h->cur = want;
+    h->drop_graphs();
+}
+int solver_reduce(cns_solver* h, int want, double* diag);
+}  // namespace cns

@@ -31,6 +31,7 @@ SIGNATURES = {
     "cns_copy_field": (ctypes.c_int, [_vp, ctypes.c_int] + [_dp] * 5),
     "cns_run": (ctypes.c_int, [_vp, ctypes.c_int] + [_dp] * 3),
     "cns_calc_rhs": (ctypes.c_int, [_vp] + [_dp] * 5),
+    "cns_set_graphs": (ctypes.c_int, [_vp, ctypes.c_int]),
     "cns_get_scalars": (ctypes.c_int, [_vp] + [_dp] * 3),
     "cns_set_scalars": (ctypes.c_int, [_vp, ctypes.c_double, ctypes.c_double, ctypes.c_double, ctypes.c_int64]),
     "cns_time_phases": (ctypes.c_int, [_vp, ctypes.c_int, _dp]),
@@ -38,6 +39,22 @@ SIGNATURES = {
     "cns_device_bytes": (ctypes.c_int64, [_vp]),
     "cns_reduce_state": (ctypes.c_int, [ctypes.c_int] * 3 + [_vp] * 7 + [ctypes.c_double] * 4 + [_vp, _vp]),
     "cns_reduce_state_noalloc": (ctypes.c_int, [ctypes.c_int] * 3 + [_vp] * 7 + [ctypes.c_double] * 4 + [_vp, _vp]),
+    "cns_batch_create": (ctypes.c_int, [ctypes.c_int] * 4 + [ctypes.c_int64, ctypes.POINTER(_vp)]),
+    "cns_batch_destroy": (ctypes.c_int, [_vp]),
+    "cns_batch_set_stream": (ctypes.c_int, [_vp, _vp]),
+    "cns_batch_add": (ctypes.c_int, [_vp, ctypes.POINTER(CnsParams)] + [_dp] * 5 +
+                      [ctypes.c_int, ctypes.POINTER(ctypes.c_int)]),
+    "cns_batch_remove": (ctypes.c_int, [_vp, ctypes.c_int]),
+    "cns_batch_member": (_vp, [_vp, ctypes.c_int]),
+    "cns_batch_get_fields": (ctypes.c_int, [_vp, ctypes.c_int] + [_dp] * 5),
+    "cns_batch_get_logs": (ctypes.c_int, [_vp, ctypes.c_int, ctypes.c_int] + [_dp] * 4),
+    "cns_batch_member_steps": (ctypes.c_int, [_vp, ctypes.c_int, ctypes.POINTER(ctypes.c_int64)]),
+    "cns_batch_info": (ctypes.c_int, [_vp, ctypes.POINTER(ctypes.c_int)] + [ctypes.POINTER(ctypes.c_int64)] * 3),
+    "cns_batch_step": (ctypes.c_int, [_vp, ctypes.c_int]),
+    "cns_batch_set_shape": (ctypes.c_int, [_vp, ctypes.c_int, ctypes.c_int]),
+    "cns_batch_get_shape": (ctypes.c_int, [_vp, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int)]),
+    "cns_batch_tune": (ctypes.c_int, [_vp, ctypes.c_int, _dp]),
+    "cns_selftest_barrier_timeout": (ctypes.c_int, [ctypes.c_int, ctypes.c_longlong, ctypes.POINTER(ctypes.c_int)]),
     "cns_probe_fma_peak": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, ctypes.c_int, _dp]),
 }
 

@@ -102,6 +102,9 @@ class Solver:
                                           _ptr(out["time"])))
         return out
 
+    def set_graphs(self, enable: bool) -> None:
+        native.check(native.lib().cns_set_graphs(self._h, int(bool(enable))))
+
     def calc_rhs(self):
         out = [np.empty(self.shape) for _ in range(5)]
         native.check(native.lib().cns_calc_rhs(self._h, *[_ptr(f) for f in out]))

@@ -164,10 +164,16 @@ CNS_API int cns_copy_field(cns_solver* h, int direction, double* r, double* u, d
  * step counter) dt and, with forcing, the body force are recomputed on the device;
  * every check_bulk steps the bulk diagnostic is evaluated. The optional host
  * arrays par1, par2, time (length nsteps) receive, per step, the bulk diagnostics
- * (kinetic energy <u.u> when not forced; bulk velocity and integral of rhoE when
- * forced; NaN on steps without a diagnostic) and the simulation time after the
- * step, as the reference's dpar1/dpar2/dtime. */
+ * (unforced: par1 = <u.u>, the reference's kinetic-energy diagnostic, and
+ * par2 = <rho |u|^2>/2; forced: bulk velocity int(rho w)/int(rho) and int(rhoE);
+ * NaN on steps without a diagnostic) and the simulation time after the step, as the
+ * reference's dpar1/dpar2/dtime. Steps are replayed from a captured CUDA graph
+ * (cns_set_graphs). */
 CNS_API int cns_run(cns_solver* h, int nsteps, double* par1, double* par2, double* time);
+
+/* Enable (default) or disable CUDA-graph replay of the time step in cns_run. The
+ * reference launches every kernel from the host; no counterpart. */
+CNS_API int cns_set_graphs(cns_solver* h, int enable);
 
 /* One evaluation of calcRHS (src/cuda_main.cu:15-42) on the current state, copied to
  * the host: d(rho)/dt, d(rho u)/dt, d(rho v)/dt, d(rho w)/dt, d(rho E)/dt. */
@@ -224,6 +230,53 @@ CNS_API int cns_reduce_state(int mx, int my, int mz, const double* r, const doub
 CNS_API int cns_reduce_state_noalloc(int mx, int my, int mz, const double* r, const double* u, const double* v,
                                      const double* w, const double* e, const double* mu, const double* dxv,
                                      double dy, double dz, double gam, double cfl, double* out, void* stream);
+
+/* ---------------------------------------------------------------------------------------
+ * Batched ensemble (no counterpart in the reference, which runs one simulation per
+ * executable): many simulations of different grid sizes and physical parameters that
+ * share the stencil orders, the precision and the Wray RK3 scheme advance together, one
+ * persistent cooperative kernel launch per Runge-Kutta stage for the whole batch, the
+ * step replayed from a captured CUDA graph. Members keep their own dt (CFL), body
+ * force, bulk schedule, time and per-step logs. Membership may change between steps
+ * (continuous batching); admission respects an optional HBM budget.
+ * ------------------------------------------------------------------------------------- */
+#define CNS_BATCH_MAX 256
+typedef struct cns_batch cns_batch;
+
+/* hbm_budget_bytes <= 0: no budget. */
+CNS_API int cns_batch_create(int device, int precision, int stencil_size, int stencil_visc,
+                             int64_t hbm_budget_bytes, cns_batch** out);
+CNS_API int cns_batch_destroy(cns_batch* b);
+CNS_API int cns_batch_set_stream(cns_batch* b, void* stream);
+/* Admit a simulation with host initial fields ([k][j][i], as cns_copy_field);
+ * max_steps sizes its per-step logs. CNS_ERR_OOM if the budget (or CNS_BATCH_MAX) would
+ * be exceeded; the batch is unchanged then. */
+CNS_API int cns_batch_add(cns_batch* b, const cns_params* p, const double* r, const double* u,
+                          const double* v, const double* w, const double* e, int max_steps, int* id_out);
+CNS_API int cns_batch_remove(cns_batch* b, int id);
+/* The member's solver handle (for cns_set_sponge, cns_get_scalars, cns_copy_field(1) ...);
+ * valid until the member is removed. NULL for an unknown id. */
+CNS_API cns_solver* cns_batch_member(cns_batch* b, int id);
+CNS_API int cns_batch_get_fields(cns_batch* b, int id, double* r, double* u, double* v, double* w, double* e);
+/* First n per-step logs of a member (as cns_run's par1/par2/time) and its current dt. */
+CNS_API int cns_batch_get_logs(cns_batch* b, int id, int n, double* par1, double* par2, double* time, double* dt);
+CNS_API int cns_batch_member_steps(cns_batch* b, int id, int64_t* steps);
+CNS_API int cns_batch_info(cns_batch* b, int* count, int64_t* points, int64_t* bytes, int64_t* launches);
+/* Advance every member by nsteps steps. */
+CNS_API int cns_batch_step(cns_batch* b, int nsteps);
+/* Launch shape of the persistent stage kernel: 128 or 256 threads per block, blocks per SM
+ * (clamped to the co-residency limit). */
+CNS_API int cns_batch_set_shape(cns_batch* b, int threads, int blocks_per_sm);
+CNS_API int cns_batch_get_shape(cns_batch* b, int* threads, int* blocks_per_sm);
+/* Autotune the launch shape by timing `steps` steps per candidate on the current members
+ * (the members advance); the choice is cached per precision, stencil orders and size
+ * class. best_ms receives the best time per step (-1 when taken from the cache). */
+CNS_API int cns_batch_tune(cns_batch* b, int steps, double* best_ms);
+
+/* Failure-detection self test (no counterpart in the reference): one block waits at the
+ * batch kernel's bounded grid barrier for a block that does not exist; the wait must give
+ * up after spin_limit (1..2^20) polls. *timed_out = 1 when it did. Nothing hangs. */
+CNS_API int cns_selftest_barrier_timeout(int device, long long spin_limit, int* timed_out);
 
 /* Measurement utility with no counterpart in the reference: dependency-free FMA
  * throughput of the FP64 (fp64 = 1) or FP32 pipe on `device`, in TFLOP/s (FMA = 2),

@@ -1,0 +1,104 @@
+"""Batched ensemble (one persistent launch per RK stage for all members): members of uneven
+size and physics against standalone solvers; a member's result is identical alone and in a
+mix; membership changes between steps; the autotuner; the bounded barrier's give-up path."""
+import ctypes
+
+import numpy as np
+import pytest
+
+from cudanavierstokes_gb300 import Solver
+from cudanavierstokes_gb300.batch import Batch
+from cudanavierstokes_gb300.initial import channel_fields, tgv_fields
+from cudanavierstokes_gb300.params import PREC_FP32_RHS, PREC_FP64, channel_params, tgv_params
+from tests._util import smooth_random_state, state_errors
+
+pytestmark = pytest.mark.gpu
+
+
+def members(prec):
+    a = tgv_params(16, precision=prec, Re=800.0)
+    b = tgv_params(24, precision=prec, my=20, mz=28, Ma=0.3, check_cfl=2)
+    c = channel_params(24, 16, 20, precision=prec, check_cfl=3, check_bulk=2)
+    fa = tgv_fields(a)
+    fb = smooth_random_state(b, seed=3)
+    fc = channel_fields(c, Solver(c).grid()["x"], seed=0)
+    return [(a, fa), (b, fb), (c, fc)]
+
+
+@pytest.mark.parametrize("prec", [PREC_FP64, PREC_FP32_RHS])
+def test_batch_matches_standalone_solvers(gpu_lib, prec):
+    ms = members(prec)
+    n = 5
+    bt = Batch(precision=prec)
+    ids = [bt.add(p, f, max_steps=16) for p, f in ms]
+    bt.step(n)
+    tol = 1e-12 if prec == PREC_FP64 else 1e-6
+    for mid, (p, f) in zip(ids, ms):
+        s = Solver(p)
+        s.copy_field_in(*f)
+        lg = s.run(n)
+        errs = state_errors(bt.fields(mid), s.copy_field_out())
+        assert max(errs) <= tol, (mid, errs)
+        lb = bt.logs(mid, n)
+        np.testing.assert_allclose(lb["time"], lg["time"], rtol=1e-12)
+        has = ~np.isnan(lg["par1"])
+        np.testing.assert_allclose(lb["par1"][has], lg["par1"][has], rtol=1e-10)
+        assert bt.steps_done(mid) == n
+
+
+def test_member_alone_equals_member_in_mix(gpu_lib):
+    ms = members(PREC_FP32_RHS)
+    alone = Batch(precision=PREC_FP32_RHS)
+    i0 = alone.add(*ms[1], max_steps=8)
+    alone.step(4)
+    mix = Batch(precision=PREC_FP32_RHS)
+    ids = [mix.add(p, f, max_steps=8) for p, f in ms]
+    mix.step(4)
+    for a, b in zip(alone.fields(i0), mix.fields(ids[1])):
+        assert np.array_equal(a, b)
+
+
+def test_membership_changes_between_steps(gpu_lib):
+    ms = members(PREC_FP64)
+    bt = Batch(precision=PREC_FP64)
+    i0 = bt.add(*ms[0], max_steps=20)
+    bt.step(2)
+    i1 = bt.add(*ms[1], max_steps=20)     # joins later (other ping-pong parity)
+    bt.step(3)
+    bt.remove(i0)
+    i2 = bt.add(*ms[2], max_steps=20)
+    bt.step(2)
+    assert bt.info()["count"] == 2
+    assert bt.steps_done(i1) == 5 and bt.steps_done(i2) == 2
+    # the late members equal standalone runs of the same length
+    for mid, (p, f), n in ((i1, ms[1], 5), (i2, ms[2], 2)):
+        s = Solver(p)
+        s.copy_field_in(*f)
+        s.run(n)
+        assert max(state_errors(bt.fields(mid), s.copy_field_out())) <= 1e-12
+
+
+def test_budget_admission(gpu_lib):
+    p, f = members(PREC_FP64)[0]
+    bt = Batch(precision=PREC_FP64, hbm_budget_bytes=1)
+    with pytest.raises(Exception):
+        bt.add(p, f, max_steps=4)
+    assert bt.info()["count"] == 0
+
+
+def test_autotune_and_shapes(gpu_lib):
+    ms = members(PREC_FP32_RHS)
+    bt = Batch(precision=PREC_FP32_RHS)
+    for p, f in ms:
+        bt.add(p, f, max_steps=64)
+    ms_best = bt.tune(2)
+    t, b = bt.shape()
+    assert t in (128, 256) and b >= 1
+    assert ms_best > 0 or ms_best == -1.0
+    bt.step(1)
+
+
+def test_bounded_barrier_gives_up(gpu_lib):
+    flag = ctypes.c_int(-1)
+    assert gpu_lib.cns_selftest_barrier_timeout(0, 2000, ctypes.byref(flag)) == 0
+    assert flag.value == 1

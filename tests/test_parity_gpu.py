@@ -84,8 +84,17 @@ def _bl_setup(oracle_mod, p):
 
 
 def test_rhs_boundary_layer(gpu_lib, oracle_mod):
+    """The boundary-layer start is near equilibrium (its net RHS is a small difference of
+    large terms), so the single-RHS comparison uses it plus 1 % smooth perturbations; the
+    unperturbed start is covered at state level by test_run_parity[bl_s3v2]."""
     p = boundary_layer_params(16, 8, 160)
     o, s = _bl_setup(oracle_mod, p)
+    base = o.get_state()
+    noise = smooth_random_state(p, seed=21, amp=0.01)
+    f = [base[0] * noise[0], base[1] + 0.01 * noise[1], base[2] + 0.01 * noise[2], base[3] + 0.01 * noise[3],
+         base[4] * noise[0]]
+    o.set_state(*f)
+    s.copy_field_in(*f)
     t = 0.37
     o.set_scalars(0.0, 0.0, t)
     s.set_scalars(0.0, 0.0, t)
@@ -211,3 +220,21 @@ def test_grid_matches_oracle(gpu_lib, oracle_mod):
         go = oracle_mod.Oracle(p).grid()
         for k in ("x", "xp", "xpp", "y", "z"):
             np.testing.assert_array_equal(g[k], go[k])
+
+
+def test_graph_replay_matches_direct_launches(gpu_lib):
+    p = channel_params(24, 16, 20).copy(check_cfl=3, check_bulk=2)
+    f = channel_fields(p, Solver(p).grid()["x"], seed=2)
+    outs, logs = [], []
+    for graphs in (True, False):
+        s = Solver(p)
+        s.set_graphs(graphs)
+        s.copy_field_in(*f)
+        logs.append(s.run(7))
+        logs.append(s.run(4))      # a second run restarts the step counter and the schedule
+        outs.append(s.copy_field_out())
+    for a, b in zip(*outs):
+        assert np.array_equal(a, b)
+    for k in ("par1", "time"):
+        np.testing.assert_array_equal(logs[0][k], logs[2][k])
+        np.testing.assert_array_equal(logs[1][k], logs[3][k])
