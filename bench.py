@@ -16,6 +16,11 @@ path is not sharded across GPUs, each rank advances its own channel).
   cpu_baseline  the CPU oracle (the reference's algorithm restated, OpenMP) on the host
               cores, on a z-slab of the same channel
   fp32_rhs    the same workload with the RHS in FP32 (state/accumulation FP64)
+  batched     48 Taylor-Green boxes of uneven size (seeded), FP32 RHS / FP64 state, one
+              persistent launch per RK stage for the whole ensemble, graph replay, autotuned
+  serving     Poisson-arrival "advance N steps" requests (Taylor-Green 32^3-192^3 and
+              64x48x64 channels, N in [50, 500]) under a 150 GB budget: p50/p99 latency and
+              aggregate Mpoint-steps/s per arrival rate
 
 --impl reference times the CPU port of the reference's path (the reference itself only
 has a GPU path) on all host cores, on the same workload and metric.
@@ -51,6 +56,8 @@ def parse_args():
     ap.add_argument("--precision", choices=["fp64", "fp32"], default="fp64")
     ap.add_argument("--no-extras", action="store_true", help="skip fp32/cpu/e2e side measurements")
     ap.add_argument("--grid", default=None, help="override the grid as MX,MY,MZ (profiling of smaller cases)")
+    ap.add_argument("--serve-requests", type=int, default=16, help="requests per arrival rate in the serving leg")
+    ap.add_argument("--serve-rates", default="1.0,3.0", help="arrival rates (requests/s) of the serving leg")
     return ap.parse_args()
 
 
@@ -181,6 +188,77 @@ def cpu_sample(p, steps_min: int = 2, seconds: float = 12.0):
     pts = q.npoints
     return pts * n / dt / 1e6, orc.max_threads(), (f"{n} RK3 steps of a {q.mx}x{q.my}x{q.mz} z-slab of the workload "
                                                     f"({pts} points, same physics and stencils), {dt:.1f} s")
+
+
+def run_batched(args, stream_ptr):
+    """BASELINE config 3: the 48-member ensemble in FP32-RHS mode."""
+    import torch
+    from cudanavierstokes_gb300.batch import Batch
+    from cudanavierstokes_gb300.workloads import ensemble, ensemble_fields
+    mem = ensemble(48, seed=0)
+    bt = Batch(precision=1)
+    bt.set_stream(stream_ptr)
+    total_steps = args.warmup + args.steps + 64
+    for p, ph in mem:
+        bt.add(p, ensemble_fields(p, ph), max_steps=total_steps)
+    tuned_ms = bt.tune(2)
+    shape = bt.shape()
+    bt.step(args.warmup)
+    info0 = bt.info()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    stream = torch.cuda.ExternalStream(stream_ptr)
+    torch.cuda.synchronize()
+    e0.record(stream)
+    bt.step(args.steps)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1)
+    info1 = bt.info()
+    pts = info1["points"]
+    out = {"value": pts * args.steps / (ms * 1e-3) / 1e6, "unit": "Mpoint-steps/s", "members": info1["count"],
+           "points": pts, "ms_per_step": ms / args.steps, "launch_shape": {"threads": shape[0],
+                                                                             "blocks_per_sm": shape[1]},
+           "tune_ms_per_step": tuned_ms, "kernel_launches_timed": info1["launches"] - info0["launches"],
+           "workload": "48 Taylor-Green boxes, edge in {32,48,64,96,128}, Re log-U[400,3200], Ma U[0.1,0.8], "
+                       "seeded phases (seed 0), 8th order, Wray RK3, FP32 RHS / FP64 state"}
+    bt.close()
+    return out
+
+
+def run_serving(args):
+    """BASELINE config 4: Poisson arrivals of advance-N-steps requests, continuous batching."""
+    import threading
+    from cudanavierstokes_gb300.server import Server
+    from cudanavierstokes_gb300.workloads import request_fields, serving_requests
+    rates = [float(r) for r in args.serve_rates.split(",") if r]
+    res = []
+    for rate in rates:
+        reqs = serving_requests(args.serve_requests, rate, seed=1)
+        fields = [request_fields(p, kind, sd) for (_, p, kind, _, sd) in reqs]   # prepared before the clock starts
+        srv = Server(precision=1, hbm_budget_bytes=150 * 10**9)
+        ids = []
+        t0 = time.perf_counter()
+
+        def submit():
+            for (ta, p, kind, n, sd), f in zip(reqs, fields):
+                dt = ta - (time.perf_counter() - t0)
+                if dt > 0:
+                    time.sleep(dt)
+                ids.append(srv.submit(p, f, n))
+        th = threading.Thread(target=submit)
+        th.start()
+        th.join()
+        for i in list(ids):
+            srv.wait(i, timeout_s=900, fetch=False)
+        wall = time.perf_counter() - t0
+        st = srv.stats()
+        srv.close()
+        res.append({"rate_per_s": rate, "requests": len(reqs), "p50_s": st["p50_s"], "p99_s": st["p99_s"],
+                    "max_s": st["max_s"], "value": st["point_steps"] / wall / 1e6, "unit": "Mpoint-steps/s",
+                    "busy_value": st["point_steps"] / max(st["busy_seconds"], 1e-9) / 1e6,
+                    "batch_steps": st["batch_steps"], "wall_s": wall})
+    return {"rates": res, "workload": "Poisson arrivals, N ~ U[50,500] steps, Taylor-Green 32^3-192^3 (Re, Ma as "
+                                      "the ensemble) and 64x48x64 channels (25 %), FP32 RHS, 150 GB HBM budget"}
 
 
 def read_traffic(N: int):
@@ -331,6 +409,10 @@ def run_gb300(args, world, rank, local):
                                 "ms_per_step": ms32 / args.steps, "phase_ms": ph32,
                                 "speedup_vs_fp64": (ms / ms32)}
             s32.close()
+        # batched ensemble and serving (FP32 RHS / FP64 state)
+        line["batched"] = run_batched(args, stream.cuda_stream)
+        line["batched"]["vs_plain_fp64"] = line["batched"]["value"] / value
+        line["serving"] = run_serving(args)
         # CPU baseline (oracle) on the host cores
         v, cores, sample = cpu_sample(p)
         line["cpu_baseline"] = {"value": v, "unit": "Mpoint-steps/s", "cores": cores, "kind": "port",

@@ -444,6 +444,20 @@ int cns_get_grid(cns_solver* h, double* x, double* xp, double* xpp, double* y, d
     return CNS_OK;
 }
 
+int cns_host_grid(const cns_params* p, double* x, double* xp, double* xpp, double* y, double* z) {
+    g_err.clear();
+    int rc = check_params(p);
+    if (rc) return rc;
+    HostGrid g;
+    build_grid(*p, g);
+    if (x) std::memcpy(x, g.x.data(), g.x.size() * 8);
+    if (xp) std::memcpy(xp, g.xp.data(), g.xp.size() * 8);
+    if (xpp) std::memcpy(xpp, g.xpp.data(), g.xpp.size() * 8);
+    if (y) std::memcpy(y, g.y.data(), g.y.size() * 8);
+    if (z) std::memcpy(z, g.z.data(), g.z.size() * 8);
+    return CNS_OK;
+}
+
 int cns_set_sponge(cns_solver* h, const double* sx, const double* sz, const double* rr, const double* ur,
                    const double* wr, const double* er) {
     if (!h) return fail(CNS_ERR_INVALID, "handle is NULL");

@@ -26,6 +26,7 @@ SIGNATURES = {
     "cns_destroy": (ctypes.c_int, [_vp]),
     "cns_set_stream": (ctypes.c_int, [_vp, _vp]),
     "cns_get_grid": (ctypes.c_int, [_vp] + [_dp] * 5),
+    "cns_host_grid": (ctypes.c_int, [ctypes.POINTER(CnsParams)] + [_dp] * 5),
     "cns_set_sponge_profiles": (ctypes.c_int, [_vp, ctypes.c_int] + [_dp] * 5 + [ctypes.c_int]),
     "cns_set_sponge": (ctypes.c_int, [_vp] + [_dp] * 6),
     "cns_copy_field": (ctypes.c_int, [_vp, ctypes.c_int] + [_dp] * 5),
@@ -57,6 +58,25 @@ SIGNATURES = {
     "cns_selftest_barrier_timeout": (ctypes.c_int, [ctypes.c_int, ctypes.c_longlong, ctypes.POINTER(ctypes.c_int)]),
     "cns_probe_fma_peak": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, ctypes.c_int, _dp]),
 }
+
+
+class ServerStats(ctypes.Structure):
+    """ctypes layout of cns_server_stats_t."""
+
+    _fields_ = [("completed", ctypes.c_int64), ("queued", ctypes.c_int64), ("running", ctypes.c_int64),
+                ("batch_steps", ctypes.c_int64), ("point_steps", ctypes.c_int64), ("busy_seconds", ctypes.c_double),
+                ("p50_s", ctypes.c_double), ("p99_s", ctypes.c_double), ("max_s", ctypes.c_double)]
+
+
+SIGNATURES.update({
+    "cns_server_create": (ctypes.c_int, [ctypes.c_int] * 4 + [ctypes.c_int64, ctypes.c_int, ctypes.POINTER(_vp)]),
+    "cns_server_destroy": (ctypes.c_int, [_vp]),
+    "cns_server_submit": (ctypes.c_int, [_vp, ctypes.POINTER(CnsParams)] + [_dp] * 5 +
+                          [ctypes.c_int, ctypes.POINTER(ctypes.c_int64)]),
+    "cns_server_poll": (ctypes.c_int, [_vp, ctypes.c_int64, ctypes.POINTER(ctypes.c_int), _dp]),
+    "cns_server_wait": (ctypes.c_int, [_vp, ctypes.c_int64, ctypes.c_double] + [_dp] * 5),
+    "cns_server_stats": (ctypes.c_int, [_vp, ctypes.POINTER(ServerStats)]),
+})
 
 
 class CnsError(RuntimeError):

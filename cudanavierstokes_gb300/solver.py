@@ -33,6 +33,15 @@ def _ptr(a):
     return a.ctypes.data_as(_dp)
 
 
+def host_grid(params: CnsParams) -> dict:
+    """Grid of these parameters computed on the host (initGrid / derivGrid), no device."""
+    p = params.copy()
+    x, xp, xpp = np.zeros(p.mx), np.zeros(p.mx), np.zeros(p.mx)
+    y, z = np.zeros(p.my), np.zeros(p.mz)
+    native.check(native.lib().cns_host_grid(ctypes.byref(p), _ptr(x), _ptr(xp), _ptr(xpp), _ptr(y), _ptr(z)))
+    return dict(x=x, xp=xp, xpp=xpp, y=y, z=z)
+
+
 class Solver:
     def __init__(self, params: CnsParams, device: int = 0):
         self.p = params.copy()

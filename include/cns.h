@@ -137,6 +137,9 @@ CNS_API int cns_set_stream(cns_solver* h, void* stream);
  * (= 1/x'(xi)), xpp[mx] (= x''(xi)), y[my], z[mz]. Any pointer may be NULL. */
 CNS_API int cns_get_grid(cns_solver* h, double* x, double* xp, double* xpp, double* y, double* z);
 
+/* The same grid computed on the host from parameters alone (no device, no handle). */
+CNS_API int cns_host_grid(const cns_params* p, double* x, double* xp, double* xpp, double* y, double* z);
+
 /* calculateSponge (src/sponge.cu:83-240) from a 1D self-similar profile
  * (the reference's blasius1D/{x,r,u,w,e}Prof.bin): sponge strengths from the sponge
  * constants, reference fields by cubic-spline interpolation of the profile at
@@ -272,6 +275,41 @@ CNS_API int cns_batch_get_shape(cns_batch* b, int* threads, int* blocks_per_sm);
  * (the members advance); the choice is cached per precision, stencil orders and size
  * class. best_ms receives the best time per step (-1 when taken from the cache). */
 CNS_API int cns_batch_tune(cns_batch* b, int steps, double* best_ms);
+
+/* ---------------------------------------------------------------------------------------
+ * Serving (no counterpart in the reference): a request loop for "advance N steps" solves
+ * with continuous batching. Requests (parameters, initial fields, N) are submitted from
+ * any thread; one worker thread owns a GPU batch, admits queued requests between steps
+ * in arrival order while the HBM budget allows, advances all resident simulations one
+ * step per tick and retires finished ones (fields copied to host memory, device memory
+ * released). Latency = submit to result ready.
+ * ------------------------------------------------------------------------------------- */
+typedef struct cns_server cns_server;
+#define CNS_REQ_QUEUED  0
+#define CNS_REQ_RUNNING 1
+#define CNS_REQ_DONE    2
+#define CNS_REQ_FAILED  3
+typedef struct cns_server_stats_t {
+    int64_t completed, queued, running;   /* requests */
+    int64_t batch_steps;                  /* batch steps taken by the worker */
+    int64_t point_steps;                  /* grid points x steps advanced */
+    double busy_seconds;                  /* first admission to last completion */
+    double p50_s, p99_s, max_s;           /* latency percentiles of completed requests */
+} cns_server_stats_t;
+
+/* max_batch <= 0: up to CNS_BATCH_MAX resident simulations. */
+CNS_API int cns_server_create(int device, int precision, int stencil_size, int stencil_visc,
+                              int64_t hbm_budget_bytes, int max_batch, cns_server** out);
+CNS_API int cns_server_destroy(cns_server* s);
+/* Copies the initial fields; thread-safe. */
+CNS_API int cns_server_submit(cns_server* s, const cns_params* p, const double* r, const double* u,
+                              const double* v, const double* w, const double* e, int nsteps, int64_t* req_id);
+CNS_API int cns_server_poll(cns_server* s, int64_t req_id, int* state, double* latency_s);
+/* Blocks up to timeout_s for the result and copies the final fields (any may be NULL);
+ * the request is forgotten afterwards. CNS_ERR_TIMEOUT if not finished in time. */
+CNS_API int cns_server_wait(cns_server* s, int64_t req_id, double timeout_s, double* r, double* u,
+                            double* v, double* w, double* e);
+CNS_API int cns_server_stats(cns_server* s, cns_server_stats_t* st);
 
 /* Failure-detection self test (no counterpart in the reference): one block waits at the
  * batch kernel's bounded grid barrier for a block that does not exist; the wait must give
