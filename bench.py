@@ -36,6 +36,8 @@ import sys
 import tempfile
 import time
 
+import numpy as np
+
 REPO = os.path.dirname(os.path.abspath(__file__))
 if REPO not in sys.path:
     sys.path.insert(0, REPO)
@@ -52,7 +54,8 @@ def parse_args():
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
-    ap.add_argument("--workload", choices=["channel", "tgv"], default="channel")
+    ap.add_argument("--workload", choices=["channel", "tgv", "precision"], default="channel")
+    ap.add_argument("--t-end", type=float, default=10.0, help="precision study: end time")
     ap.add_argument("--precision", choices=["fp64", "fp32"], default="fp64")
     ap.add_argument("--no-extras", action="store_true", help="skip fp32/cpu/e2e side measurements")
     ap.add_argument("--grid", default=None, help="override the grid as MX,MY,MZ (profiling of smaller cases)")
@@ -261,6 +264,65 @@ def run_serving(args):
                                       "the ensemble) and 64x48x64 channels (25 %), FP32 RHS, 150 GB HBM budget"}
 
 
+def ke_series(p, fields, t_end, chunk=250):
+    """Run to t_end logging, every step, the state's time and <u.u>, <rho|u|^2>/2 (the
+    bulk diagnostic is evaluated on the state at the start of each step)."""
+    from cudanavierstokes_gb300 import Solver
+    s = Solver(p.copy(check_bulk=1))
+    s.copy_field_in(*fields)
+    t_prev, ts, k1, k2 = 0.0, [], [], []
+    t0 = time.perf_counter()
+    while True:
+        lg = s.run(chunk)
+        tt = np.concatenate([[t_prev], lg["time"][:-1]])
+        ts.append(tt); k1.append(lg["par1"]); k2.append(lg["par2"])
+        t_prev = float(lg["time"][-1])
+        if t_prev >= t_end:
+            break
+    wall = time.perf_counter() - t0
+    out = dict(t=np.concatenate(ts), ke=np.concatenate(k1), ke_rho=np.concatenate(k2), wall=wall,
+               steps=int(sum(len(a) for a in ts)))
+    s.close()
+    return out
+
+
+def at_time(t, y, t0):
+    """Value and derivative at t0 of the cubic through the 4 samples around t0."""
+    i = int(np.searchsorted(t, t0))
+    sl = slice(max(i - 2, 0), max(i - 2, 0) + 4)
+    c = np.polyfit(t[sl] - t0, y[sl], 3)
+    return float(c[-1]), float(c[-2])
+
+
+def run_precision(args):
+    """BASELINE config 2: Taylor-Green to t_end, FP32 RHS (FP64 state, accumulation, T/p
+    recovery, reductions) against all-FP64; relative error of <u.u>, <rho|u|^2>/2 and of the
+    dissipation rate eps = -dK/dt at t_end (K = <rho|u|^2>/2)."""
+    from cudanavierstokes_gb300.initial import tgv_fields
+    from cudanavierstokes_gb300.params import tgv_params
+    n = int(args.grid.split(",")[0]) if args.grid else 128
+    p64 = tgv_params(n)
+    f = tgv_fields(p64)
+    r64 = ke_series(p64, f, args.t_end)
+    r32 = ke_series(p64.copy(precision=1), f, args.t_end)
+    res = {}
+    for key in ("ke", "ke_rho"):
+        a, da = at_time(r64["t"], r64[key], args.t_end)
+        b, db = at_time(r32["t"], r32[key], args.t_end)
+        res[key] = {"fp64": a, "fp32_rhs": b, "rel_err": abs(b - a) / abs(a),
+                    "eps_fp64": -da, "eps_fp32_rhs": -db, "eps_rel_err": abs(db - da) / abs(da)}
+    line = {"metric": "kinetic-energy relative error at t_end, FP32 RHS vs FP64", "value": res["ke_rho"]["rel_err"],
+            "unit": "relative", "higher_is_better": False, "dtype": "f32-rhs/f64-state vs f64",
+            "data": "synthetic", "config": {"workload": f"Taylor-Green {n}^3, Ma 0.1, Re 1600, Pr 0.71, S=V=4, "
+                                                        "Wray RK3, CFL 0.5", "t_end": args.t_end},
+            "ke_uu": res["ke"], "ke_rho": res["ke_rho"],
+            "fp64": {"steps": r64["steps"], "wall_s": r64["wall"],
+                     "Mpoint_steps_per_s": p64.npoints * r64["steps"] / r64["wall"] / 1e6},
+            "fp32_rhs": {"steps": r32["steps"], "wall_s": r32["wall"],
+                         "Mpoint_steps_per_s": p64.npoints * r32["steps"] / r32["wall"] / 1e6}}
+    print(json.dumps(line), flush=True)
+
+
 def read_traffic(N: int):
     """Per-launch DRAM bytes of the RHS kernel from the committed ncu summary (scaled to this
     grid by points if the capture was taken on a smaller case)."""
@@ -424,7 +486,10 @@ def run_gb300(args, world, rank, local):
 def main():
     args = parse_args()
     world, rank, local = dist_setup()
-    if args.impl == "reference":
+    if args.workload == "precision":
+        if rank == 0:
+            run_precision(args)
+    elif args.impl == "reference":
         run_reference(args, world, rank)
     else:
         run_gb300(args, world, rank, local)
