@@ -19,6 +19,8 @@ CSRC = os.path.join(PKG, "csrc")
 LIBDIR = os.path.join(PKG, "_lib")
 OBJDIR = os.path.join(LIBDIR, "obj")
 LIB = os.path.join(LIBDIR, "libcns_gb300.so")
+DRIVER = os.path.join(LIBDIR, "cns")
+DRIVER_SRC = os.path.join(PKG, "csrc", "cns_main.cpp")
 INCLUDE = os.path.join(REPO, "include")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
@@ -35,7 +37,9 @@ def nvcc() -> str:
 
 
 def sources():
-    return sorted(glob.glob(os.path.join(CSRC, "*.cu")) + glob.glob(os.path.join(CSRC, "*.cpp")))
+    """Library translation units (the driver's main() is linked separately)."""
+    return sorted(f for f in glob.glob(os.path.join(CSRC, "*.cu")) + glob.glob(os.path.join(CSRC, "*.cpp"))
+                  if f != DRIVER_SRC)
 
 
 def headers():
@@ -83,6 +87,13 @@ def build(verbose: bool = False, force: bool = False) -> str:
         if r.returncode != 0:
             raise RuntimeError(f"link failed:\n{r.stderr[-4000:]}")
         os.replace(tmp, LIB)
+    if _stale(DRIVER, [LIB, DRIVER_SRC] + headers()):
+        cmd = ["g++", "-O2", "-std=c++17", "-I" + INCLUDE, "-o", DRIVER + ".tmp", DRIVER_SRC, "-L" + LIBDIR,
+               "-lcns_gb300", "-Wl,-rpath,$ORIGIN"]
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError(f"driver build failed:\n{r.stderr[-4000:]}")
+        os.replace(DRIVER + ".tmp", DRIVER)
     return LIB
 
 

@@ -1,0 +1,83 @@
+"""The drop-in driver executable (the reference's main: parameter file with globals.h names,
+fields/%c.%07d.bin output, restart, solution.txt)."""
+import os
+import subprocess
+
+import numpy as np
+import pytest
+
+from cudanavierstokes_gb300 import build
+from cudanavierstokes_gb300.initial import read_fields, tgv_reference_fields
+from cudanavierstokes_gb300.params import tgv_params
+from cudanavierstokes_gb300.solver import host_grid
+
+PARAMS = """# Taylor-Green box, reference parameter names
+mx_tot = 16
+my_tot = 20
+mz_tot = 24
+Lx = 6.283185307179586
+Ly = 6.283185307179586
+Lz = 6.283185307179586
+stencilSize = 4
+stencilVisc = 4
+nsteps = {nsteps}
+nfiles = {nfiles}
+restartFile = {restart}
+CFL = 0.5
+Re = 1600.0
+Pr = 0.71
+Ma = 0.1
+viscexp = 1.0
+gam = 1.4
+checkCFLcondition = 100
+checkBulk = 2
+"""
+
+
+def _run(tmp_path, nsteps=4, nfiles=2, restart=-1):
+    build.build()
+    pf = tmp_path / "params.txt"
+    pf.write_text(PARAMS.format(nsteps=nsteps, nfiles=nfiles, restart=restart))
+    return subprocess.run([build.DRIVER, str(pf), str(tmp_path)], capture_output=True, text=True, timeout=600)
+
+
+def _gpu_available():
+    try:
+        import torch
+        return torch.cuda.is_available()
+    except Exception:
+        return False
+
+
+def test_driver_fails_loudly_without_gpu(tmp_path):
+    if _gpu_available():
+        pytest.skip("a GPU is present")
+    r = _run(tmp_path)
+    assert r.returncode == 2 and "no CUDA device" in r.stderr
+    p = tgv_params(16).copy(my=20, mz=24)
+    np.testing.assert_array_equal(np.fromfile(tmp_path / "fields" / "x.bin"), host_grid(p)["x"])
+
+
+@pytest.mark.gpu
+def test_driver_matches_library_and_restarts(tmp_path, gpu_lib):
+    from cudanavierstokes_gb300 import Solver
+    r = _run(tmp_path, nsteps=4, nfiles=2)
+    assert r.returncode == 0, r.stderr
+    p = tgv_params(16).copy(my=20, mz=24, check_bulk=2)
+    out2 = read_fields(str(tmp_path / "fields"), 2, p.shape)
+    s = Solver(p)
+    s.copy_field_in(*tgv_reference_fields(p))
+    s.run(4)
+    s.run(4)
+    for a, b in zip(out2, s.copy_field_out()):
+        np.testing.assert_array_equal(a, b)
+    assert (tmp_path / "solution.txt").read_text().strip()
+    # restart from file 1 for one file reproduces file 2
+    out_dir = tmp_path / "restart"
+    (out_dir / "fields").mkdir(parents=True)
+    for c in "ruvwe":
+        os.link(tmp_path / "fields" / f"{c}.0000001.bin", out_dir / "fields" / f"{c}.0000001.bin")
+    r = _run(out_dir, nsteps=4, nfiles=1, restart=1)
+    assert r.returncode == 0, r.stderr
+    for a, b in zip(read_fields(str(out_dir / "fields"), 2, p.shape), out2):
+        np.testing.assert_array_equal(a, b)
