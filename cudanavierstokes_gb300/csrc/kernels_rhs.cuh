@@ -76,18 +76,38 @@ __device__ __forceinline__ void rhs_direction(const Geom& g, const CoefT<R>& cf,
     diss = fma(tau[1], Gr[3 * DIR + 1], diss);
     diss = fma(tau[2], dw, diss);
 
+    // velocity stencils, loaded once for the viscous second derivatives and the fluxes
+    R us[2 * S + 1], vs[2 * S + 1], ws[2 * S + 1];
+    us[S] = u0; vs[S] = v0; ws[S] = w0;
+#pragma unroll
+    for (int l = 1; l <= S; l++) {
+        us[S + l] = ld(in.u, c + l * st); us[S - l] = ld(in.u, c - l * st);
+        vs[S + l] = ld(in.v, c + l * st); vs[S - l] = ld(in.v, c - l * st);
+        ws[S + l] = ld(in.w, c + l * st); ws[S - l] = ld(in.w, c - l * st);
+    }
     // d mu/dx s_{DIR,c} + mu d2 u_c/dx2
     const R dmu = d1<R, V>(in.m, c, st, c1V) * xpi;
     R d2uu, d2vv, d2ww, d2tt;
     if (nux) {
-        d2uu = d2x_nu<R, V>(in.u, c, cf.cvsx, g.mx, i);
-        d2vv = d2x_nu<R, V>(in.v, c, cf.cvsx, g.mx, i);
-        d2ww = d2x_nu<R, V>(in.w, c, cf.cvsx, g.mx, i);
+        R a = (R)0, b = (R)0, e2 = (R)0;
+#pragma unroll
+        for (int it = 0; it < 2 * V + 1; it++) {
+            const R cw = __ldg(cf.cvsx + it * g.mx + i);
+            a = fma(cw, us[S + it - V], a);
+            b = fma(cw, vs[S + it - V], b);
+            e2 = fma(cw, ws[S + it - V], e2);
+        }
+        d2uu = a; d2vv = b; d2ww = e2;
         d2tt = d2x_nu<R, V>(in.t, c, cf.cvsx, g.mx, i);
     } else {
-        d2uu = d2u<R, V>(in.u, c, st, c2V);
-        d2vv = d2u<R, V>(in.v, c, st, c2V);
-        d2ww = d2u<R, V>(in.w, c, st, c2V);
+        R a = c2V[0] * us[S], b = c2V[0] * vs[S], e2 = c2V[0] * ws[S];
+#pragma unroll
+        for (int k = 1; k <= V; k++) {
+            a = fma(c2V[k], us[S + k] + us[S - k], a);
+            b = fma(c2V[k], vs[S + k] + vs[S - k], b);
+            e2 = fma(c2V[k], ws[S + k] + ws[S - k], e2);
+        }
+        d2uu = a; d2vv = b; d2ww = e2;
         d2tt = d2u<R, V>(in.t, c, st, c2V);
     }
     W[0] = fma(tau[0], dmu, fma(d2uu, m0, W[0]));
@@ -115,9 +135,9 @@ __device__ __forceinline__ void rhs_direction(const Geom& g, const CoefT<R>& cf,
     for (int l = 1; l <= S; l++) {
         const long long o = l * st;
         const R rm = ld(in.r, c - o), rp = ld(in.r, c + o);
-        const R um = ld(in.u, c - o), up = ld(in.u, c + o);
-        const R vm = ld(in.v, c - o), vp = ld(in.v, c + o);
-        const R wm = ld(in.w, c - o), wp = ld(in.w, c + o);
+        const R um = us[S - l], up = us[S + l];
+        const R vm = vs[S - l], vp = vs[S + l];
+        const R wm = ws[S - l], wp = ws[S + l];
         const R hm = ld(in.h, c - o), hp = ld(in.h, c + o);
         const R gm = DIR == 0 ? um : (DIR == 1 ? vm : wm);
         const R gp = DIR == 0 ? up : (DIR == 1 ? vp : wp);
@@ -193,14 +213,22 @@ __device__ __forceinline__ void rhs_point(const Geom& g, const CoefT<R>& cf, con
         return;
     }
     // ---- stage update: the RHS combination in R, the accumulation into the state in FP64 ----
+    // The register arrays are read in full before any of them is written: the compiler
+    // cannot prove that rb[q] and rb[q+1] (or k2) do not overlap, so interleaved
+    // load/store pairs would serialise five memory round trips at the end of every thread.
     const double dt = scal[SC_DT];
     double qn[5];
     if (up.kind == ST_LS) {
         const double q0[5] = {rr, uu * rr, vv * rr, ww * rr, ee};
         const R a = (R)up.a, b = (R)up.b;
+        R prev[5] = {0, 0, 0, 0, 0};
+        if (up.a != 0.0) {
+#pragma unroll
+            for (int q = 0; q < 5; q++) prev[q] = up.rb[q][c];
+        }
 #pragma unroll
         for (int q = 0; q < 5; q++) {
-            const R x = up.a != 0.0 ? fma(a, up.rb[q][c], b * acc[q]) : b * acc[q];
+            const R x = up.a != 0.0 ? fma(a, prev[q], b * acc[q]) : b * acc[q];
             qn[q] = fma(dt, (double)x, q0[q]);
             up.rb[q][c] = acc[q];
         }
@@ -215,17 +243,23 @@ __device__ __forceinline__ void rhs_point(const Geom& g, const CoefT<R>& cf, con
         }
     } else {
         double q0[5];
+        R k1[5] = {0, 0, 0, 0, 0}, kk[5] = {0, 0, 0, 0, 0};
+        const bool use_k1 = up.kind == ST_C2 || up.kind == ST_C3, use_k2 = up.kind != ST_C2;
 #pragma unroll
-        for (int q = 0; q < 5; q++) q0[q] = up.q0[q][c];
+        for (int q = 0; q < 5; q++) {
+            q0[q] = up.q0[q][c];
+            if (use_k1) k1[q] = up.rb[q][c];
+            if (use_k2) kk[q] = up.k2[q][c];
+        }
 #pragma unroll
         for (int q = 0; q < 5; q++) {
             const double Rd = (double)acc[q];
             switch (up.kind) {
-            case ST_C2: qn[q] = q0[q] + (2 * Rd - (double)up.rb[q][c]) * dt; up.k2[q][c] = acc[q]; break;
-            case ST_C3: qn[q] = q0[q] + dt * ((double)up.rb[q][c] + 4 * (double)up.k2[q][c] + Rd) / 6.; break;
-            case ST_R4_2: up.k2[q][c] = (R)((double)up.k2[q][c] + 2.0 * Rd); qn[q] = q0[q] + 0.5 * dt * Rd; break;
-            case ST_R4_3: up.k2[q][c] = (R)((double)up.k2[q][c] + 2.0 * Rd); qn[q] = q0[q] + dt * Rd; break;
-            default: qn[q] = q0[q] + dt / 6.0 * ((double)up.k2[q][c] + Rd); break;
+            case ST_C2: qn[q] = q0[q] + (2 * Rd - (double)k1[q]) * dt; up.k2[q][c] = acc[q]; break;
+            case ST_C3: qn[q] = q0[q] + dt * ((double)k1[q] + 4 * (double)kk[q] + Rd) / 6.; break;
+            case ST_R4_2: up.k2[q][c] = (R)((double)kk[q] + 2.0 * Rd); qn[q] = q0[q] + 0.5 * dt * Rd; break;
+            case ST_R4_3: up.k2[q][c] = (R)((double)kk[q] + 2.0 * Rd); qn[q] = q0[q] + dt * Rd; break;
+            default: qn[q] = q0[q] + dt / 6.0 * ((double)kk[q] + Rd); break;
             }
         }
     }
@@ -238,7 +272,7 @@ __device__ __forceinline__ void rhs_point(const Geom& g, const CoefT<R>& cf, con
 }
 
 template <typename R, int S, int V>
-__global__ void __launch_bounds__(128) k_rhs(Geom g, CoefT<R> cf, RhsIn<R> in, Update<R> up,
+__global__ void __launch_bounds__(128, sizeof(R) == 4 ? 6 : 4) k_rhs(Geom g, CoefT<R> cf, RhsIn<R> in, Update<R> up,
                                              const double* __restrict__ scal, int quirk) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     const int j = blockIdx.y * blockDim.y + threadIdx.y;
