@@ -167,7 +167,7 @@ __global__ void __launch_bounds__(256, sizeof(R) == 4 ? 2 : 1) k_batch_stage(con
             in.h = I.der[0]; in.t = I.der[1]; in.p = I.der[2]; in.m = I.der[3]; in.l = I.der[4]; in.dil = I.dil;
             for (int c = 0; c < 9; c++) in.g[c] = I.grad[c];
             Update<R> up;
-            up.kind = kind; up.a = a; up.b = b;
+            up.kind = kind; up.a = a; up.b = b; up.ca = (R)a; up.cb = (R)b; up.use_prev = a != 0.0;
             up.qin = StateIn{I.q[cur][0], I.q[cur][1], I.q[cur][2], I.q[cur][3], I.q[cur][4]};
             const int nx = 1 - cur;
             up.qout = StateOut{I.q[nx][0], I.q[nx][1], I.q[nx][2], I.q[nx][3], I.q[nx][4]};

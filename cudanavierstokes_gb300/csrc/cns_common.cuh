@@ -44,6 +44,8 @@ struct Phys {
     int vexp_is_one, quirk, perturbed;
     int pert_kc, pert_lp;
     double pert_amp1, pert_amp2, pert_omega1, pert_omega2, pert_lambda;
+    // FP32 copies for the FP32-RHS state kernel (converted once on the host)
+    float f_Rgas, f_cvInv, f_invRe, f_clam, f_vexp;
 };
 
 // Stencil coefficients premultiplied by the inverse grid spacing of each direction,
@@ -80,11 +82,53 @@ __device__ __forceinline__ bool wall_perturbation(const Phys& ph, double dy_inv,
     return true;
 }
 
+// FP64 <-> FP32 conversions on the integer ALUs. The hardware conversions issue on the
+// FP64 pipe, which on this part runs at 1/64 of the FP32 rate and bounds the FP32-RHS
+// kernels, so they are done with bit operations on the IEEE 754 binary64 / binary32
+// layouts (sign | exponent | fraction; biases 1023 and 127), without branches:
+//   double -> float: the result keeps the 8 low exponent bits with bit 7 flipped
+//     (e - 896 = e ^ 0x80 mod 256 for 897 <= e <= 1150) and the 23 leading fraction bits,
+//     rounded half to even on the 29 discarded bits; the carry of the rounding runs into
+//     the exponent (and to infinity at the top of the range), as the format intends;
+//   float -> double: exact, exponent + 896 and the fraction shifted by 29.
+// Results equal __double2float_rn and (double)f bit for bit, except that a result or an
+// input in the binary32 subnormal range (below 2^-126 in magnitude) becomes a signed zero
+// and every NaN becomes the quiet NaN of its sign.
+__device__ __forceinline__ float d2f(double x) {
+    const unsigned hi = (unsigned)__double2hiint(x), lo = (unsigned)__double2loint(x);
+    const unsigned ah = hi & 0x7fffffffu;
+    unsigned body = (__funnelshift_l(lo, hi, 3) & 0x7fffffffu) ^ 0x40000000u;
+    body += ((lo & 0x1fffffffu) + (body & 1u) + 0x0fffffffu) >> 29;
+    body = ah < 0x38100000u ? 0u : body;                                    // |x| < 2^-126
+    body = ah >= 0x47f00000u ? 0x7f800000u : body;                          // |x| >= 2^128, inf
+    body = (ah > 0x7ff00000u || (ah == 0x7ff00000u && lo != 0u)) ? 0x7fc00000u : body;   // NaN
+    return __uint_as_float((hi & 0x80000000u) | body);
+}
+
+__device__ __forceinline__ double f2d(float f) {
+    const unsigned b = __float_as_uint(f), a = b & 0x7fffffffu;
+    const bool tiny = a < 0x00800000u, special = a >= 0x7f800000u;
+    unsigned hi = (a >> 3) + 0x38000000u, lo = a << 29;
+    hi = tiny ? 0u : (special ? ((a >> 3) | 0x7ff00000u) : hi);
+    lo = tiny ? 0u : lo;
+    return __hiloint2double((int)((b & 0x80000000u) | hi), (int)lo);
+}
+
+// conversions between FP64 and the arithmetic type R of a kernel
+template <typename R>
+__device__ __forceinline__ R to_r(double x) {
+    if constexpr (sizeof(R) == 4) return d2f(x); else return x;
+}
+template <typename R>
+__device__ __forceinline__ double to_d(R x) {
+    if constexpr (sizeof(R) == 4) return f2d(x); else return x;
+}
+
 // Reciprocal of a double: FP32 seed refined by two Newton steps (error squared each
 // step: 2^-24 -> 2^-48 -> 2^-96), within one ulp of 1/x. Valid for 1e-37 < |x| < 1e37,
 // the range of densities; cheaper than the IEEE division on the FP64 pipe.
 __device__ __forceinline__ double rcp_nr(double x) {
-    double r = (double)__frcp_rn(__double2float_rn(x));
+    double r = f2d(__frcp_rn(d2f(x)));
     double e = fma(-x, r, 1.0);
     r = fma(r, e, r);
     e = fma(-x, r, 1.0);

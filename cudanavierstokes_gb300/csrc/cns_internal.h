@@ -58,6 +58,8 @@ template <typename R>
 struct Update {
     int kind;
     double a, b;            // low-storage coefficients
+    R ca, cb;               // the same in R (no per-thread conversion)
+    int use_prev;           // a != 0: the previous stage's RHS enters the combination
     StateIn qin;            // state at the stage start (point values only)
     StateOut qout;          // new state (interior)
     R* rb[5];               // RHS register (low storage: R_prev in, R out; classic: k1)

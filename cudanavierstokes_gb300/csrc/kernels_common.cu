@@ -77,7 +77,7 @@ __global__ void __launch_bounds__(RED_THREADS) k_reduce_partial(Geom g, Phys ph,
             double sos = sqrt(ph.gam * (ph.gam - 1) * ien);
             double dx = g.dxv[i];
             double d2x = dx * dx;
-            double m = (double)mu[c];
+            double m = to_d<R>(mu[c]);
             double ci = fmax((fabs(uu) + sos) / dx, fmax((fabs(vv) + sos) * g.dy, (fabs(ww) + sos) * g.dz));
             double vi = fmax(m / d2x, fmax(m * g.d2y, m * g.d2z));
             dtmin = fmin(dtmin, ph.cfl / fmax(ci, vi));

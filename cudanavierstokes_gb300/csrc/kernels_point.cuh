@@ -22,23 +22,27 @@ __device__ __forceinline__ void state_point(const Geom& g, const Phys& ph, const
     const double T = ph.cvInv * en;
     const double pr = rr * ph.Rgas * T;
     const double hh = (ee + pr) * inv;
-    o.t[c] = (R)T;
-    o.p[c] = (R)pr;
-    o.h[c] = (R)hh;
+    const R Tr = to_r<R>(T);
+    o.t[c] = Tr;
+    o.p[c] = to_r<R>(pr);
+    o.h[c] = to_r<R>(hh);
     if constexpr (sizeof(R) == 4) {
-        const float Tf = (float)T;
-        const float suth = ph.vexp_is_one ? Tf : powf(Tf, (float)ph.vexp);
-        o.m[c] = suth * (float)ph.invRe;
-        o.l[c] = suth * (float)ph.clam;
+        const float Tf = Tr;
+        const float suth = ph.vexp_is_one ? Tf : powf(Tf, ph.f_vexp);
+        o.m[c] = suth * ph.f_invRe;
+        o.l[c] = suth * ph.f_clam;
+        const float rf = d2f(rr);
+        if (o.r32) {
+            o.r32[c] = rf; o.u32[c] = d2f(uu); o.v32[c] = d2f(vv); o.w32[c] = d2f(ww);
+        }
+        // the positivity test on the FP32 roundings keeps it off the FP64 pipe
+        if (!(Tf > 0.f) || !(rf > 0.f)) scal[SC_NONFINITE] = 1.0;   // racy flag write, any writer is fine
     } else {
         const double suth = ph.vexp_is_one ? T : pow(T, ph.vexp);
         o.m[c] = (R)(suth * ph.invRe);
         o.l[c] = (R)(suth * ph.clam);
+        if (!(T > 0.0) || !(rr > 0.0)) scal[SC_NONFINITE] = 1.0;   // racy flag write, any writer is fine
     }
-    if (o.r32) {
-        o.r32[c] = (R)rr; o.u32[c] = (R)uu; o.v32[c] = (R)vv; o.w32[c] = (R)ww;
-    }
-    if (!(T > 0.0) || !(rr > 0.0)) scal[SC_NONFINITE] = 1.0;   // racy flag write, any writer is fine
 }
 
 // Stage 0 of a step advances the simulation time by dt (deviceAdvanceTime) and, with a
@@ -99,7 +103,7 @@ __device__ __forceinline__ void ghost_state_cell(const Geom& g, const Phys& ph, 
             pg = f.p[cp];
             Tg = f.t[cp];
             double pv;
-            if (ph.perturbed && wall_perturbation(ph, g.dy, j, k, scal[SC_TIME], &pv)) ug = (R)pv;
+            if (ph.perturbed && wall_perturbation(ph, g.dy, j, k, scal[SC_TIME], &pv)) ug = to_r<R>(pv);
         } else {                  // boundary layer, free stream: extrapolate through the last node
             const long long cl = g.at(g.mx - 1, j, k);
             const long long cm = g.at(g.mx - 1 - m, j, k);

@@ -125,9 +125,14 @@ __device__ __forceinline__ void rhs_direction(const Geom& g, const CoefT<R>& cf,
 
     // split-form convective derivatives, telescoped (see file comment); with a uniform
     // spacing the flux weights already carry 1/2 or 1/4 and 1/dx, so they accumulate
-    // straight into the RHS
+    // straight into the RHS. With Q-(l) = (rho_{-l}+rho_0)(g_{-l}+g_0) and
+    // Q+(l) = (rho_0+rho_l)(g_0+g_l), the cubic flux of phi is
+    //   sum_l a_l [Q-(phi_{-l}+phi_0) - Q+(phi_0+phi_l)]
+    //     = sum_l [(a_l Q-) phi_{-l} - (a_l Q+) phi_l]  +  phi_0 sum_l a_l (Q- - Q+),
+    // and the last sum is half the mass flux (fq = 2 fc), so the products a_l Q+- are
+    // shared by the four cubic fluxes: 18 instead of 28 operations per l.
     const R un = DIR == 0 ? u0 : (DIR == 1 ? v0 : w0);
-    R fr = nux ? (R)0 : acc[0], fu = nux ? (R)0 : acc[1], fv = nux ? (R)0 : acc[2], fw = nux ? (R)0 : acc[3],
+    R sq = (R)0, fu = nux ? (R)0 : acc[1], fv = nux ? (R)0 : acc[2], fw = nux ? (R)0 : acc[3],
       fe = nux ? (R)0 : acc[4];
     const R* fq = cf.fq[DIR];
     const R* fcb = cf.fc[DIR];
@@ -143,13 +148,19 @@ __device__ __forceinline__ void rhs_direction(const Geom& g, const CoefT<R>& cf,
         const R gp = DIR == 0 ? up : (DIR == 1 ? vp : wp);
         const R Qm = (rm + r0) * (gm + un);
         const R Qp = (r0 + rp) * (un + gp);
-        const R a = fcb[l];
-        fr = fma(fq[l], Qm - Qp, fr);
-        fu = fma(a, fma(Qm, um + u0, -Qp * (u0 + up)), fu);
-        fv = fma(a, fma(Qm, vm + v0, -Qp * (v0 + vp)), fv);
-        fw = fma(a, fma(Qm, wm + w0, -Qp * (w0 + wp)), fw);
-        fe = fma(a, fma(Qm, hm + h0, -Qp * (h0 + hp)), fe);
+        sq = fma(fq[l], Qm - Qp, sq);
+        const R am = fcb[l] * Qm, ap = fcb[l] * Qp;
+        fu = fma(am, um, fma(-ap, up, fu));
+        fv = fma(am, vm, fma(-ap, vp, fv));
+        fw = fma(am, wm, fma(-ap, wp, fw));
+        fe = fma(am, hm, fma(-ap, hp, fe));
     }
+    const R half = (R)0.5 * sq;
+    fu = fma(u0, half, fu);
+    fv = fma(v0, half, fv);
+    fw = fma(w0, half, fw);
+    fe = fma(h0, half, fe);
+    const R fr = nux ? sq : acc[0] + sq;
     if (nux) {
         acc[0] = fma(xpi, fr, acc[0]);
         acc[1] = fma(xpi, fu, acc[1]);
@@ -186,12 +197,12 @@ __device__ __forceinline__ void rhs_point(const Geom& g, const CoefT<R>& cf, con
     acc[4] += fma(m0, diss, cond) + fma(u0, W[0], fma(v0, W[1], w0 * W[2]));
 
     // ---- body force and sponge (RHS terms, arithmetic type R) ----
-    const R dpdz = (R)scal[SC_DPDZ];
+    const R dpdz = to_r<R>(scal[SC_DPDZ]);
     acc[3] += dpdz;
     acc[4] = fma(dpdz, w0, acc[4]);
     const double rr = up.qin.r[c], uu = up.qin.u[c], vv = up.qin.v[c], ww = up.qin.w[c], ee = up.qin.e[c];
     if (up.spx) {
-        const R sg = (R)(up.spx[i] + up.spz[k]);
+        const R sg = to_r<R>(up.spx[i] + up.spz[k]);
         const long long i2 = (long long)i + (long long)k * g.mx;
         if constexpr (sizeof(R) == 8) {
             acc[0] += sg * (up.rref[i2] - rr);
@@ -200,11 +211,11 @@ __device__ __forceinline__ void rhs_point(const Geom& g, const CoefT<R>& cf, con
             acc[3] += sg * (up.wref[i2] - rr * ww);
             acc[4] += sg * (up.eref[i2] - ee);
         } else {
-            acc[0] += sg * ((R)up.rref[i2] - r0);
-            acc[1] += sg * ((R)up.uref[i2] - r0 * u0);
-            acc[2] += sg * ((R)up.vref[i2] - r0 * v0);
-            acc[3] += sg * ((R)up.wref[i2] - r0 * w0);
-            acc[4] += sg * ((R)up.eref[i2] - (R)ee);
+            acc[0] += sg * (to_r<R>(up.rref[i2]) - r0);
+            acc[1] += sg * (to_r<R>(up.uref[i2]) - r0 * u0);
+            acc[2] += sg * (to_r<R>(up.vref[i2]) - r0 * v0);
+            acc[3] += sg * (to_r<R>(up.wref[i2]) - r0 * w0);
+            acc[4] += sg * (to_r<R>(up.eref[i2]) - to_r<R>(ee));
         }
     }
     if (up.kind == ST_RHS_ONLY) {
@@ -220,16 +231,16 @@ __device__ __forceinline__ void rhs_point(const Geom& g, const CoefT<R>& cf, con
     double qn[5];
     if (up.kind == ST_LS) {
         const double q0[5] = {rr, uu * rr, vv * rr, ww * rr, ee};
-        const R a = (R)up.a, b = (R)up.b;
+        const R a = up.ca, b = up.cb;
         R prev[5] = {0, 0, 0, 0, 0};
-        if (up.a != 0.0) {
+        if (up.use_prev) {
 #pragma unroll
             for (int q = 0; q < 5; q++) prev[q] = up.rb[q][c];
         }
 #pragma unroll
         for (int q = 0; q < 5; q++) {
-            const R x = up.a != 0.0 ? fma(a, prev[q], b * acc[q]) : b * acc[q];
-            qn[q] = fma(dt, (double)x, q0[q]);
+            const R x = up.use_prev ? fma(a, prev[q], b * acc[q]) : b * acc[q];
+            qn[q] = fma(dt, to_d<R>(x), q0[q]);
             up.rb[q][c] = acc[q];
         }
     } else if (up.kind == ST_C1 || up.kind == ST_R4_1) {
@@ -237,7 +248,7 @@ __device__ __forceinline__ void rhs_point(const Geom& g, const CoefT<R>& cf, con
 #pragma unroll
         for (int q = 0; q < 5; q++) {
             up.q0[q][c] = q0[q];
-            const double Rd = (double)acc[q];
+            const double Rd = to_d<R>(acc[q]);
             if (up.kind == ST_C1) { qn[q] = q0[q] + Rd * dt / 2.0; up.rb[q][c] = acc[q]; }
             else { qn[q] = q0[q] + 0.5 * dt * Rd; up.k2[q][c] = acc[q]; }
         }
@@ -253,13 +264,13 @@ __device__ __forceinline__ void rhs_point(const Geom& g, const CoefT<R>& cf, con
         }
 #pragma unroll
         for (int q = 0; q < 5; q++) {
-            const double Rd = (double)acc[q];
+            const double Rd = to_d<R>(acc[q]);
             switch (up.kind) {
-            case ST_C2: qn[q] = q0[q] + (2 * Rd - (double)k1[q]) * dt; up.k2[q][c] = acc[q]; break;
-            case ST_C3: qn[q] = q0[q] + dt * ((double)k1[q] + 4 * (double)kk[q] + Rd) / 6.; break;
-            case ST_R4_2: up.k2[q][c] = (R)((double)kk[q] + 2.0 * Rd); qn[q] = q0[q] + 0.5 * dt * Rd; break;
-            case ST_R4_3: up.k2[q][c] = (R)((double)kk[q] + 2.0 * Rd); qn[q] = q0[q] + dt * Rd; break;
-            default: qn[q] = q0[q] + dt / 6.0 * ((double)kk[q] + Rd); break;
+            case ST_C2: qn[q] = q0[q] + (2 * Rd - to_d<R>(k1[q])) * dt; up.k2[q][c] = acc[q]; break;
+            case ST_C3: qn[q] = q0[q] + dt * (to_d<R>(k1[q]) + 4 * to_d<R>(kk[q]) + Rd) / 6.; break;
+            case ST_R4_2: up.k2[q][c] = to_r<R>(to_d<R>(kk[q]) + 2.0 * Rd); qn[q] = q0[q] + 0.5 * dt * Rd; break;
+            case ST_R4_3: up.k2[q][c] = to_r<R>(to_d<R>(kk[q]) + 2.0 * Rd); qn[q] = q0[q] + dt * Rd; break;
+            default: qn[q] = q0[q] + dt / 6.0 * (to_d<R>(kk[q]) + Rd); break;
             }
         }
     }

@@ -3,6 +3,7 @@
 #include <cuda_runtime.h>
 
 #include "../../include/cns.h"
+#include "cns_common.cuh"
 
 namespace {
 
@@ -44,7 +45,45 @@ int probe(int device, int iters, double* tflops) {
     return CNS_OK;
 }
 
+__global__ void __launch_bounds__(256) k_convert(const double* __restrict__ x, float* __restrict__ f_alu,
+                                                 float* __restrict__ f_hw, const float* __restrict__ y,
+                                                 double* __restrict__ d_alu, double* __restrict__ d_hw, long long n) {
+    for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x) {
+        f_alu[t] = cns::d2f(x[t]);
+        f_hw[t] = __double2float_rn(x[t]);
+        d_alu[t] = cns::f2d(y[t]);
+        d_hw[t] = (double)y[t];
+    }
+}
+
 }  // namespace
+
+extern "C" int cns_selftest_convert(int device, const double* x, const float* y, long long n, float* f_alu,
+                                    float* f_hw, double* d_alu, double* d_hw) {
+    if (!x || !y || !f_alu || !f_hw || !d_alu || !d_hw || n < 1 || n > (1LL << 28)) return CNS_ERR_INVALID;
+    if (cudaSetDevice(device) != cudaSuccess) return CNS_ERR_CUDA;
+    char* buf = nullptr;
+    const size_t nb = (size_t)n;
+    if (cudaMalloc(&buf, nb * (8 + 4 + 4 + 4 + 8 + 8)) != cudaSuccess) return CNS_ERR_OOM;
+    double* dx = (double*)buf;
+    double* dda = dx + nb;
+    double* ddh = dda + nb;
+    float* dfa = (float*)(ddh + nb);
+    float* dfh = dfa + nb;
+    float* dy = dfh + nb;
+    cudaError_t e = cudaMemcpy(dx, x, nb * 8, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(dy, y, nb * 4, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) {
+        k_convert<<<1024, 256>>>(dx, dfa, dfh, dy, dda, ddh, n);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = cudaMemcpy(f_alu, dfa, nb * 4, cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess) e = cudaMemcpy(f_hw, dfh, nb * 4, cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess) e = cudaMemcpy(d_alu, dda, nb * 8, cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess) e = cudaMemcpy(d_hw, ddh, nb * 8, cudaMemcpyDeviceToHost);
+    cudaFree(buf);
+    return e == cudaSuccess ? CNS_OK : CNS_ERR_CUDA;
+}
 
 extern "C" int cns_probe_fma_peak(int device, int fp64, int iters, double* tflops) {
     if (!tflops || iters < 10) return CNS_ERR_INVALID;

@@ -157,6 +157,9 @@ int rhs_phase(cns_solver* h, int kind, double a, double b) {
     up.kind = kind;
     up.a = a;
     up.b = b;
+    up.ca = (R)a;
+    up.cb = (R)b;
+    up.use_prev = a != 0.0;
     up.qin = state_in(h, h->cur);
     const int nb = 1 - h->cur;
     up.qout = StateOut{h->q[nb][0], h->q[nb][1], h->q[nb][2], h->q[nb][3], h->q[nb][4]};
@@ -374,6 +377,8 @@ int cns_create(const cns_params* pin, int device, cns_solver** out) {
     ph.pert_amp1 = p.pert_amp1; ph.pert_amp2 = p.pert_amp2;
     ph.pert_omega1 = p.Re * p.pert_omega1_per_re; ph.pert_omega2 = p.pert_omega2;
     ph.pert_lambda = p.Ly / (2.0 * M_PI);
+    ph.f_Rgas = (float)ph.Rgas; ph.f_cvInv = (float)ph.cvInv; ph.f_invRe = (float)ph.invRe;
+    ph.f_clam = (float)ph.clam; ph.f_vexp = (float)ph.vexp;
 
     for (int d = 0; d < 3; d++)
         for (int k = 0; k < 5; k++) {

@@ -322,6 +322,12 @@ CNS_API int cns_selftest_barrier_timeout(int device, long long spin_limit, int* 
  * roofline next to the measured HBM bandwidth. */
 CNS_API int cns_probe_fma_peak(int device, int fp64, int iters, double* tflops);
 
+/* Self test with no counterpart in the reference: the solver's FP64 -> FP32 and FP32 ->
+ * FP64 conversions, which run on the integer units, next to the hardware conversions on
+ * the same inputs (n <= 2^28 values each; host arrays). Bitwise equality is the contract. */
+CNS_API int cns_selftest_convert(int device, const double* x, const float* y, long long n, float* f_alu, float* f_hw,
+                                 double* d_alu, double* d_hw);
+
 #ifdef __cplusplus
 }
 #endif
