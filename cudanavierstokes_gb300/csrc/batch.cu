@@ -142,7 +142,8 @@ BatchInst<R> make_inst(cns_solver* h, int rows, int64_t cap) {
     I.tlog = h->tlog;
     for (int c = 0; c < 2; c++)
         for (int f = 0; f < 5; f++) I.q[c][f] = h->q[c][f];
-    for (int f = 0; f < 5; f++) { I.der[f] = (R*)h->der[f]; I.rb[f] = (R*)h->rb[f]; }
+    for (int f = 0; f < 4; f++) I.der[f] = (R*)h->der[f];
+    for (int f = 0; f < 5; f++) I.rb[f] = (R*)h->rb[f];
     for (int f = 0; f < 4; f++) I.s32[f] = h->fp32 ? (R*)h->s32[f] : nullptr;
     I.dil = (R*)h->dil;
     for (int f = 0; f < 9; f++) I.grad[f] = (R*)h->grad[f];

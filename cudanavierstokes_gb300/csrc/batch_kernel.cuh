@@ -27,7 +27,7 @@ struct BatchInst {
     double* tlog;
     long long tcap;     // capacity of tlog
     double* q[2][5];
-    R* der[5];      // h, t, p, mu, lambda
+    R* der[4];      // h, t, p, mu
     R* s32[4];      // FP32 stencil copies of rho, u, v, w (FP32-RHS mode) or nullptr
     R* dil;
     R* grad[9];
@@ -102,7 +102,7 @@ __global__ void __launch_bounds__(256, sizeof(R) == 4 ? 2 : 1) k_batch_stage(con
         if (stage0 && lu == 0 && threadIdx.x == 0)
             advance_time(I.scal, (long long)I.scal[SC_STEP] < I.tcap ? I.tlog : nullptr);
         if (i < I.g.mx && j < I.g.my) {
-            DerivedOut<R> o{I.der[0], I.der[1], I.der[2], I.der[3], I.der[4], I.s32[0], I.s32[1], I.s32[2], I.s32[3]};
+            DerivedOut<R> o{I.der[0], I.der[1], I.der[2], I.der[3], I.s32[0], I.s32[1], I.s32[2], I.s32[3]};
             state_point<R>(I.g, I.ph, StateIn{I.q[cur][0], I.q[cur][1], I.q[cur][2], I.q[cur][3], I.q[cur][4]}, o,
                            I.scal, i, j, k);
         }
@@ -119,7 +119,7 @@ __global__ void __launch_bounds__(256, sizeof(R) == 4 ? 2 : 1) k_batch_stage(con
             else {
                 f.r = (R*)I.q[cur][0]; f.u = (R*)I.q[cur][1]; f.v = (R*)I.q[cur][2]; f.w = (R*)I.q[cur][3];
             }
-            f.h = I.der[0]; f.t = I.der[1]; f.p = I.der[2]; f.m = I.der[3]; f.l = I.der[4];
+            f.h = I.der[0]; f.t = I.der[1]; f.p = I.der[2]; f.m = I.der[3];
             ghost_state_cell<R>(I.g, I.ph, f, I.scal, t);
         }
     }
@@ -164,7 +164,7 @@ __global__ void __launch_bounds__(256, sizeof(R) == 4 ? 2 : 1) k_batch_stage(con
                 in.r = (const R*)I.q[cur][0]; in.u = (const R*)I.q[cur][1];
                 in.v = (const R*)I.q[cur][2]; in.w = (const R*)I.q[cur][3];
             }
-            in.h = I.der[0]; in.t = I.der[1]; in.p = I.der[2]; in.m = I.der[3]; in.l = I.der[4]; in.dil = I.dil;
+            in.h = I.der[0]; in.t = I.der[1]; in.p = I.der[2]; in.m = I.der[3]; in.dil = I.dil;
             for (int c = 0; c < 9; c++) in.g[c] = I.grad[c];
             Update<R> up;
             up.kind = kind; up.a = a; up.b = b; up.ca = (R)a; up.cb = (R)b; up.use_prev = a != 0.0;

@@ -45,7 +45,7 @@ struct Phys {
     int pert_kc, pert_lp;
     double pert_amp1, pert_amp2, pert_omega1, pert_omega2, pert_lambda;
     // FP32 copies for the FP32-RHS state kernel (converted once on the host)
-    float f_Rgas, f_cvInv, f_invRe, f_clam, f_vexp;
+    float f_Rgas, f_cvInv, f_invRe, f_vexp;
 };
 
 // Stencil coefficients premultiplied by the inverse grid spacing of each direction,
@@ -62,6 +62,7 @@ struct CoefT {
     R c2V[3][5];
     R fq[3][5];      // 0.5  * c1S: split-form quadratic flux (rho u) weights
     R fc[3][5];      // 0.25 * c1S: split-form cubic flux (rho u phi) weights
+    R lam_mu;        // lambda / mu = 1 / (Pr Ec)
     const R* xp;     // [mx]
     const R* cvsx;   // [(2V+1)*mx], index it*mx + i
 };
@@ -135,8 +136,60 @@ __device__ __forceinline__ double rcp_nr(double x) {
     return fma(r, e, r);
 }
 
+// x^a in FP64 for the viscosity law mu ~ T^a, as exp(a ln x) with
+//   ln x = k ln2 + 2 atanh(s),  x = 2^k m,  m in [sqrt(2)/2, sqrt(2)),  s = (m-1)/(m+1),
+//     atanh s = s + s^3/3 + ... + s^23/23  (|s| <= 0.172: truncation below 2^-64),
+//   exp y = 2^j exp(r),  j = nearest(y / ln2),  r = y - j ln2 with ln2 split in a 32-bit
+//     head (j ln2_hi exact) and a tail (Cody & Waite's additive range reduction),
+//     exp r = sum r^n / n!, n <= 13  (|r| <= 0.347: truncation below 2^-57).
+// About 40 FP64 operations against ~120 for the library pow, which runs on the FP64
+// pipe. The error of exp(y) is that of y, about |y| ulp, so the series serve
+// |a ln x| < 1 (T^0.7 for 0.24 < T < 4.2, the temperatures of these flows), within a
+// few ulp of pow (a GPU test bounds it); other arguments take pow itself.
+__device__ __forceinline__ double pow_visc(double x, double a) {
+    const double LN2_HI = 0.6931471803691238, LN2_LO = 1.9082149292705877e-10;
+    const double INV_LN2 = 1.4426950408889634, SHIFT = 6755399441055744.0;   // 1.5 * 2^52
+    if (!(x > 1e-300 && x < 1e300)) return pow(x, a);
+    const unsigned hx = (unsigned)__double2hiint(x);
+    int k = (int)(hx >> 20) - 1023;
+    unsigned hm = (hx & 0x000fffffu) | 0x3ff00000u;        // m in [1, 2)
+    if (hm >= 0x3ff6a09fu) { hm -= 0x00100000u; k += 1; }  // m in [0.707, 1.414]
+    const double m = __hiloint2double((int)hm, __double2loint(x));
+    const double num = m - 1.0, den = m + 1.0;               // m - 1 exact
+    double inv = f2d(__frcp_rn(d2f(den)));
+    inv = fma(inv, fma(-den, inv, 1.0), inv);
+    inv = fma(inv, fma(-den, inv, 1.0), inv);
+    const double s = num * inv, z = s * s;
+    double p = 1.0 / 23.0;
+    p = fma(p, z, 1.0 / 21.0); p = fma(p, z, 1.0 / 19.0);
+    p = fma(p, z, 1.0 / 17.0); p = fma(p, z, 1.0 / 15.0); p = fma(p, z, 1.0 / 13.0);
+    p = fma(p, z, 1.0 / 11.0); p = fma(p, z, 1.0 / 9.0);  p = fma(p, z, 1.0 / 7.0);
+    p = fma(p, z, 1.0 / 5.0);  p = fma(p, z, 1.0 / 3.0);
+    const double lnm = fma(2.0 * s * z, p, 2.0 * s);         // 2 atanh(s)
+    // k as a double through the 2^52 + 2^31 bias (no conversion instruction)
+    const double kd = __hiloint2double(0x43300000, (int)((unsigned)k + 0x80000000u)) -
+                      __hiloint2double(0x43300000, (int)0x80000000u);
+    const double lnx = fma(kd, LN2_HI, fma(kd, LN2_LO, lnm));
+    const double y = a * lnx;
+    if (!(fabs(y) < 1.0)) return pow(x, a);
+    const double t = fma(y, INV_LN2, SHIFT);
+    const int j = __double2loint(t);
+    const double jd = t - SHIFT;
+    double r = fma(-jd, LN2_HI, y);
+    r = fma(-jd, LN2_LO, r);
+    double e = 1.0 / 6227020800.0;                                      // 1/13!
+    e = fma(e, r, 1.0 / 479001600.0); e = fma(e, r, 1.0 / 39916800.0);  // 1/12!, 1/11!
+    e = fma(e, r, 1.0 / 3628800.0);   e = fma(e, r, 1.0 / 362880.0);
+    e = fma(e, r, 1.0 / 40320.0);     e = fma(e, r, 1.0 / 5040.0);
+    e = fma(e, r, 1.0 / 720.0);       e = fma(e, r, 1.0 / 120.0);
+    e = fma(e, r, 1.0 / 24.0);        e = fma(e, r, 1.0 / 6.0);
+    e = fma(e, r, 0.5);               e = fma(e, r, 1.0);
+    e = fma(e, r, 1.0);
+    return __hiloint2double(__double2hiint(e) + (int)((unsigned)j << 20), __double2loint(e));
+}
+
 template <typename R> __device__ __forceinline__ R cns_pow(R a, R b);
-template <> __device__ __forceinline__ double cns_pow<double>(double a, double b) { return pow(a, b); }
+template <> __device__ __forceinline__ double cns_pow<double>(double a, double b) { return pow_visc(a, b); }
 template <> __device__ __forceinline__ float cns_pow<float>(float a, float b) { return powf(a, b); }
 
 }  // namespace cns

@@ -16,16 +16,19 @@ struct StateOut {
     double *r, *u, *v, *w, *e;
 };
 
+// lambda = mu / (Pr Ec) at every point, ghosts included (wall and extrapolated ghosts
+// are formed from the same T or linearly), so only mu is stored and the RHS applies
+// the ratio once per point
 template <typename R>
 struct DerivedOut {
-    R *h, *t, *p, *m, *l;
+    R *h, *t, *p, *m;
     R *r32, *u32, *v32, *w32;   // FP32-RHS stencil copies (nullptr in FP64 mode)
 };
 
-// the nine ghosted stencil inputs
+// the eight ghosted stencil inputs
 template <typename R>
 struct StencilFields {
-    R *r, *u, *v, *w, *t, *p, *h, *m, *l;
+    R *r, *u, *v, *w, *t, *p, *h, *m;
 };
 
 template <typename R>
@@ -37,7 +40,7 @@ struct GradOut {
 // RHS stage kernel inputs
 template <typename R>
 struct RhsIn {
-    const R *r, *u, *v, *w, *t, *p, *h, *m, *l, *dil;
+    const R *r, *u, *v, *w, *t, *p, *h, *m, *dil;
     const R* g[9];
 };
 

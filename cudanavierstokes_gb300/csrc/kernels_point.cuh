@@ -8,9 +8,10 @@
 namespace cns {
 
 // ---------------------------------------------------------------------------------
-// State recovery (calcState, src/cuda_main.cu:218-242): T, p, H, mu, lambda from
-// rho, u, v, w, rhoE in FP64; stored as R. In FP32-RHS mode the FP32 stencil copies of
-// rho, u, v, w are written too and mu, lambda are evaluated in FP32 from the FP64 T.
+// State recovery (calcState, src/cuda_main.cu:218-242): T, p, H, mu from rho, u, v, w,
+// rhoE in FP64; stored as R (lambda = mu / (Pr Ec) is applied in the RHS). In FP32-RHS
+// mode the FP32 stencil copies of rho, u, v, w are written too and mu is evaluated in
+// FP32 from the FP64 T.
 // ---------------------------------------------------------------------------------
 template <typename R>
 __device__ __forceinline__ void state_point(const Geom& g, const Phys& ph, const StateIn& q, const DerivedOut<R>& o,
@@ -30,7 +31,6 @@ __device__ __forceinline__ void state_point(const Geom& g, const Phys& ph, const
         const float Tf = Tr;
         const float suth = ph.vexp_is_one ? Tf : powf(Tf, ph.f_vexp);
         o.m[c] = suth * ph.f_invRe;
-        o.l[c] = suth * ph.f_clam;
         const float rf = d2f(rr);
         if (o.r32) {
             o.r32[c] = rf; o.u32[c] = d2f(uu); o.v32[c] = d2f(vv); o.w32[c] = d2f(ww);
@@ -38,9 +38,8 @@ __device__ __forceinline__ void state_point(const Geom& g, const Phys& ph, const
         // the positivity test on the FP32 roundings keeps it off the FP64 pipe
         if (!(Tf > 0.f) || !(rf > 0.f)) scal[SC_NONFINITE] = 1.0;   // racy flag write, any writer is fine
     } else {
-        const double suth = ph.vexp_is_one ? T : pow(T, ph.vexp);
+        const double suth = ph.vexp_is_one ? T : pow_visc(T, ph.vexp);
         o.m[c] = (R)(suth * ph.invRe);
-        o.l[c] = (R)(suth * ph.clam);
         if (!(T > 0.0) || !(rr > 0.0)) scal[SC_NONFINITE] = 1.0;   // racy flag write, any writer is fine
     }
 }
@@ -63,10 +62,10 @@ __host__ __device__ __forceinline__ long long ghost_count(const Geom& g) {
 }
 
 // ---------------------------------------------------------------------------------
-// Ghost cell t of the stencil inputs rho, u, v, w, T, p, H, mu, lambda.
+// Ghost cell t of the stencil inputs rho, u, v, w, T, p, H, mu.
 //   x: periodic | isothermal wall (BCxNumber1/3: p even, u v w odd, T = 2Tw - T,
-//      mu, lambda, rho, H from the ghost p, T, u, v, w) | boundary layer (bottom: p, T
-//      even, u v w odd, u perturbed; top: linear extrapolation; mu, lambda, rho, H derived)
+//      mu, rho, H from the ghost p, T, u, v, w) | boundary layer (bottom: p, T
+//      even, u v w odd, u perturbed; top: linear extrapolation; mu, rho, H derived)
 //   y: periodic.   z: periodic | linear extrapolation about the end nodes.
 // (src/boundary.h:38-188, src/boundary_condition_x.h:47-115, _y.h:19-58, _z.h:80-332)
 // Only the six faces are filled (no stencil reads an edge or a corner).
@@ -76,7 +75,7 @@ __device__ __forceinline__ void ghost_state_cell(const Geom& g, const Phys& ph, 
                                                  const double* scal, long long t) {
     const long long G = g.G;
     const long long nx = 2 * G * g.my * g.mz, ny = 2 * G * g.mx * g.mz, nz = 2 * G * g.mx * g.my;
-    R* F[9] = {f.r, f.u, f.v, f.w, f.t, f.p, f.h, f.m, f.l};
+    R* F[8] = {f.r, f.u, f.v, f.w, f.t, f.p, f.h, f.m};
     if (t < nx) {
         const int m = (int)(t % G) + 1; t /= G;
         const int side = (int)(t % 2); t /= 2;
@@ -87,7 +86,7 @@ __device__ __forceinline__ void ghost_state_cell(const Geom& g, const Phys& ph, 
         if (g.xbc == XBC_PER) {
             const long long cs = g.at(side == 0 ? g.mx - m : m - 1, j, k);
 #pragma unroll
-            for (int q = 0; q < 9; q++) F[q][cg] = F[q][cs];
+            for (int q = 0; q < 8; q++) F[q][cg] = F[q][cs];
             return;
         }
         const int ip = side == 0 ? m - 1 : g.mx - m;
@@ -116,7 +115,6 @@ __device__ __forceinline__ void ghost_state_cell(const Geom& g, const Phys& ph, 
         const R suth = ph.vexp_is_one ? Tg : cns_pow<R>(Tg, (R)ph.vexp);
         f.u[cg] = ug; f.v[cg] = vg; f.w[cg] = wg; f.p[cg] = pg; f.t[cg] = Tg;
         f.m[cg] = suth * (R)ph.invRe;
-        f.l[cg] = suth * (R)ph.clam;
         f.h[cg] = Tg * (R)ph.hcoef + (R)0.5 * (ug * ug + vg * vg + wg * wg);
         f.r[cg] = pg / ((R)ph.Rgas * Tg);
         return;
@@ -130,7 +128,7 @@ __device__ __forceinline__ void ghost_state_cell(const Geom& g, const Phys& ph, 
         const long long cg = g.at(i, side == 0 ? -m : g.my - 1 + m, k);
         const long long cs = g.at(i, side == 0 ? g.my - m : m - 1, k);
 #pragma unroll
-        for (int q = 0; q < 9; q++) F[q][cg] = F[q][cs];
+        for (int q = 0; q < 8; q++) F[q][cg] = F[q][cs];
         return;
     }
     t -= ny;
@@ -143,12 +141,12 @@ __device__ __forceinline__ void ghost_state_cell(const Geom& g, const Phys& ph, 
         if (!g.zbl) {
             const long long cs = g.at(i, j, side == 0 ? g.mz - m : m - 1);
 #pragma unroll
-            for (int q = 0; q < 9; q++) F[q][cg] = F[q][cs];
+            for (int q = 0; q < 8; q++) F[q][cg] = F[q][cs];
         } else {
             const long long c0 = g.at(i, j, side == 0 ? 0 : g.mz - 1);
             const long long cm = g.at(i, j, side == 0 ? m : g.mz - 1 - m);
 #pragma unroll
-            for (int q = 0; q < 9; q++) F[q][cg] = (R)2.0 * F[q][c0] - F[q][cm];
+            for (int q = 0; q < 8; q++) F[q][cg] = (R)2.0 * F[q][c0] - F[q][cm];
         }
     }
 }

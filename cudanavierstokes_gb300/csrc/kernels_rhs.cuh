@@ -56,7 +56,7 @@ __device__ __forceinline__ R d2x_nu(const R* __restrict__ f, long long c, const 
 // and the mu multiplications are applied once per point instead of once per direction.
 template <typename R, int S, int V, int DIR>
 __device__ __forceinline__ void rhs_direction(const Geom& g, const CoefT<R>& cf, const RhsIn<R>& in, long long c,
-                                              int i, const R (&Gr)[9], R th0, R m0, R m3, R l0, R u0, R v0, R w0,
+                                              int i, const R (&Gr)[9], R th0, R m0, R m3, R u0, R v0, R w0,
                                               R r0, R h0, int quirk, R (&acc)[5], R (&W)[3], R& diss, R& cond) {
     const long long st = DIR == 0 ? 1LL : (DIR == 1 ? g.P : g.PS);
     const bool nux = (DIR == 0) && g.nonuniform_x;
@@ -113,11 +113,11 @@ __device__ __forceinline__ void rhs_direction(const Geom& g, const CoefT<R>& cf,
     W[0] = fma(tau[0], dmu, fma(d2uu, m0, W[0]));
     W[1] = fma(tau[1], dmu, fma(d2vv, m0, W[1]));
     W[2] = fma(tau[2], dmu, fma(d2ww, m0, W[2]));
-    // heat conduction: lambda d2T + dlambda dT
-    const R dl = d1<R, V>(in.l, c, st, c1V) * xpi;
+    // heat conduction lambda d2T + dlambda dT = (lambda/mu) (mu d2T + dmu dT); the ratio
+    // is applied once per point
     const R dt = d1<R, V>(in.t, c, st, c1V) * xpi;
-    cond = fma(d2tt, l0, cond);
-    cond = fma(dt, dl, cond);
+    cond = fma(d2tt, m0, cond);
+    cond = fma(dt, dmu, cond);
     // mu/3 d(theta) on the DIR momentum (and its work), pressure gradient
     const R dth = d1<R, V>(in.dil, c, st, c1V) * xpi;
     const R dp = d1<R, S>(in.p, c, st, c1S) * xpi;
@@ -182,19 +182,19 @@ __device__ __forceinline__ void rhs_point(const Geom& g, const CoefT<R>& cf, con
     R Gr[9];
 #pragma unroll
     for (int q = 0; q < 9; q++) Gr[q] = ld(in.g[q], c);
-    const R th0 = ld(in.dil, c), m0 = ld(in.m, c), l0 = ld(in.l, c);
+    const R th0 = ld(in.dil, c), m0 = ld(in.m, c);
     const R u0 = ld(in.u, c), v0 = ld(in.v, c), w0 = ld(in.w, c), r0 = ld(in.r, c), h0 = ld(in.h, c);
     const R m3 = m0 * (R)(1.0 / 3.0);
     R acc[5] = {0, 0, 0, 0, 0};
     R W[3] = {0, 0, 0};
     R diss = 0, cond = 0;
-    rhs_direction<R, S, V, 0>(g, cf, in, c, i, Gr, th0, m0, m3, l0, u0, v0, w0, r0, h0, quirk, acc, W, diss, cond);
-    rhs_direction<R, S, V, 1>(g, cf, in, c, i, Gr, th0, m0, m3, l0, u0, v0, w0, r0, h0, quirk, acc, W, diss, cond);
-    rhs_direction<R, S, V, 2>(g, cf, in, c, i, Gr, th0, m0, m3, l0, u0, v0, w0, r0, h0, quirk, acc, W, diss, cond);
+    rhs_direction<R, S, V, 0>(g, cf, in, c, i, Gr, th0, m0, m3, u0, v0, w0, r0, h0, quirk, acc, W, diss, cond);
+    rhs_direction<R, S, V, 1>(g, cf, in, c, i, Gr, th0, m0, m3, u0, v0, w0, r0, h0, quirk, acc, W, diss, cond);
+    rhs_direction<R, S, V, 2>(g, cf, in, c, i, Gr, th0, m0, m3, u0, v0, w0, r0, h0, quirk, acc, W, diss, cond);
     acc[1] += W[0];
     acc[2] += W[1];
     acc[3] += W[2];
-    acc[4] += fma(m0, diss, cond) + fma(u0, W[0], fma(v0, W[1], w0 * W[2]));
+    acc[4] += fma(m0, diss, cf.lam_mu * cond) + fma(u0, W[0], fma(v0, W[1], w0 * W[2]));
 
     // ---- body force and sponge (RHS terms, arithmetic type R) ----
     const R dpdz = to_r<R>(scal[SC_DPDZ]);

@@ -103,7 +103,7 @@ RhsIn<R> rhs_in(cns_solver* h) {
         in.v = (const R*)h->q[h->cur][2]; in.w = (const R*)h->q[h->cur][3];
     }
     in.h = (const R*)h->der[0]; in.t = (const R*)h->der[1]; in.p = (const R*)h->der[2];
-    in.m = (const R*)h->der[3]; in.l = (const R*)h->der[4]; in.dil = (const R*)h->dil;
+    in.m = (const R*)h->der[3]; in.dil = (const R*)h->dil;
     for (int q = 0; q < 9; q++) in.g[q] = (const R*)h->grad[q];
     return in;
 }
@@ -116,7 +116,7 @@ StateIn state_in(cns_solver* h, int b) {
 template <typename R>
 int state_phase(cns_solver* h, int advance_time, double* time_log) {
     DerivedOut<R> o;
-    o.h = (R*)h->der[0]; o.t = (R*)h->der[1]; o.p = (R*)h->der[2]; o.m = (R*)h->der[3]; o.l = (R*)h->der[4];
+    o.h = (R*)h->der[0]; o.t = (R*)h->der[1]; o.p = (R*)h->der[2]; o.m = (R*)h->der[3];
     o.r32 = o.u32 = o.v32 = o.w32 = nullptr;
     StencilFields<R> f;
     if (h->fp32) {
@@ -125,7 +125,7 @@ int state_phase(cns_solver* h, int advance_time, double* time_log) {
     } else {
         f.r = (R*)h->q[h->cur][0]; f.u = (R*)h->q[h->cur][1]; f.v = (R*)h->q[h->cur][2]; f.w = (R*)h->q[h->cur][3];
     }
-    f.t = o.t; f.p = o.p; f.h = o.h; f.m = o.m; f.l = o.l;
+    f.t = o.t; f.p = o.p; f.h = o.h; f.m = o.m;
     launch_state<R>(h->geom, h->phys, state_in(h, h->cur), o, h->scal, advance_time, time_log, h->stream);
     launch_ghost_state<R>(h->geom, h->phys, f, h->scal, h->stream);
     h->launches += 2;
@@ -378,7 +378,7 @@ int cns_create(const cns_params* pin, int device, cns_solver** out) {
     ph.pert_omega1 = p.Re * p.pert_omega1_per_re; ph.pert_omega2 = p.pert_omega2;
     ph.pert_lambda = p.Ly / (2.0 * M_PI);
     ph.f_Rgas = (float)ph.Rgas; ph.f_cvInv = (float)ph.cvInv; ph.f_invRe = (float)ph.invRe;
-    ph.f_clam = (float)ph.clam; ph.f_vexp = (float)ph.vexp;
+    ph.f_vexp = (float)ph.vexp;
 
     for (int d = 0; d < 3; d++)
         for (int k = 0; k < 5; k++) {
@@ -388,6 +388,9 @@ int cns_create(const cns_params* pin, int device, cns_solver** out) {
             h->cf64.fq[d][k] = h->hg.fq[d][k]; h->cf64.fc[d][k] = h->hg.fc[d][k];
             h->cf32.fq[d][k] = (float)h->hg.fq[d][k]; h->cf32.fc[d][k] = (float)h->hg.fc[d][k];
         }
+    // lambda = mu / (Pr Ec)  (calcState, src/cuda_main.cu:218-242)
+    h->cf64.lam_mu = 1.0 / (p.Pr * ph.Ec);
+    h->cf32.lam_mu = (float)h->cf64.lam_mu;
 
     CK(cudaStreamCreateWithFlags(&h->own_stream, cudaStreamNonBlocking));
     h->stream = h->own_stream;
@@ -396,7 +399,7 @@ int cns_create(const cns_params* pin, int device, cns_solver** out) {
     const size_t N = (size_t)p.mx * p.my * p.mz;
     for (int b = 0; b < 2 && !rc; b++)
         for (int f = 0; f < 5 && !rc; f++) rc = h->alloc_field((void**)&h->q[b][f], 8);
-    for (int f = 0; f < 5 && !rc; f++) rc = h->alloc_field(&h->der[f], rs);
+    for (int f = 0; f < 4 && !rc; f++) rc = h->alloc_field(&h->der[f], rs);
     if (!rc && h->fp32)
         for (int f = 0; f < 4 && !rc; f++) rc = h->alloc_field(&h->s32[f], 4);
     if (!rc) rc = h->alloc_field(&h->dil, rs);

@@ -35,7 +35,7 @@ struct cns_solver {
 
     double* q[2][5] = {};        // state ping-pong (rho, u, v, w, rhoE)
     int cur = 0;
-    void* der[5] = {};           // h, t, p, mu, lambda   (R)
+    void* der[4] = {};           // h, t, p, mu   (R)
     void* s32[4] = {};           // FP32 stencil copies of rho, u, v, w
     void* dil = nullptr;         // (R)
     void* grad[9] = {};          // (R)

@@ -324,9 +324,15 @@ CNS_API int cns_probe_fma_peak(int device, int fp64, int iters, double* tflops);
 
 /* Self test with no counterpart in the reference: the solver's FP64 -> FP32 and FP32 ->
  * FP64 conversions, which run on the integer units, next to the hardware conversions on
- * the same inputs (n <= 2^28 values each; host arrays). Bitwise equality is the contract. */
+ * the same inputs (n <= 2^28 values each; host arrays). The contract: bitwise equal,
+ * except that magnitudes below 2^-126 become a zero of the same sign and NaN stays NaN. */
 CNS_API int cns_selftest_convert(int device, const double* x, const float* y, long long n, float* f_alu, float* f_hw,
                                  double* d_alu, double* d_hw);
+
+/* Self test with no counterpart in the reference: the solver's FP64 power for the
+ * viscosity law (T^viscexp) next to the CUDA library pow on the same n <= 2^27 host
+ * values. */
+CNS_API int cns_selftest_pow(int device, const double* x, long long n, double a, double* fast, double* lib);
 
 #ifdef __cplusplus
 }
