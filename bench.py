@@ -194,36 +194,52 @@ def cpu_sample(p, steps_min: int = 2, seconds: float = 12.0):
 
 
 def run_batched(args, stream_ptr):
-    """BASELINE config 3: the 48-member ensemble in FP32-RHS mode."""
+    """BASELINE config 3: the 48-member ensemble in FP32-RHS mode, in the execution mode and
+    launch shape the autotuner picks; the other mode is timed beside it for the record."""
     import torch
     from cudanavierstokes_gb300.batch import Batch
     from cudanavierstokes_gb300.workloads import ensemble, ensemble_fields
     mem = ensemble(48, seed=0)
     bt = Batch(precision=1)
     bt.set_stream(stream_ptr)
-    total_steps = args.warmup + args.steps + 64
+    total_steps = 2 * args.warmup + 2 * args.steps + 128
     for p, ph in mem:
         bt.add(p, ensemble_fields(p, ph), max_steps=total_steps)
     tuned_ms = bt.tune(2)
-    shape = bt.shape()
-    bt.step(args.warmup)
-    info0 = bt.info()
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     stream = torch.cuda.ExternalStream(stream_ptr)
-    torch.cuda.synchronize()
-    e0.record(stream)
-    bt.step(args.steps)
-    e1.record(stream)
-    torch.cuda.synchronize()
-    ms = e0.elapsed_time(e1)
-    info1 = bt.info()
-    pts = info1["points"]
-    out = {"value": pts * args.steps / (ms * 1e-3) / 1e6, "unit": "Mpoint-steps/s", "members": info1["count"],
-           "points": pts, "ms_per_step": ms / args.steps, "launch_shape": {"threads": shape[0],
-                                                                             "blocks_per_sm": shape[1]},
-           "tune_ms_per_step": tuned_ms, "kernel_launches_timed": info1["launches"] - info0["launches"],
+
+    def timed():
+        bt.step(args.warmup)
+        info0 = bt.info()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        e0.record(stream)
+        bt.step(args.steps)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1), bt.info()["launches"] - info0["launches"]
+
+    mode, shape = bt.mode(), bt.shape()
+    ms, launches = timed()
+    pts = bt.info()["points"]
+    names = {0: "persistent (one cooperative launch per RK stage for all members)",
+             1: "concurrent (members' step graphs on 16 streams)"}
+    out = {"value": pts * args.steps / (ms * 1e-3) / 1e6, "unit": "Mpoint-steps/s", "members": bt.info()["count"],
+           "points": pts, "ms_per_step": ms / args.steps, "mode": names[mode],
+           "launch_shape": {"threads": shape[0], "blocks_per_sm": shape[1]} if mode == 0 else None,
+           "tune_ms_per_step": tuned_ms, "kernel_launches_timed": launches,
            "workload": "48 Taylor-Green boxes, edge in {32,48,64,96,128}, Re log-U[400,3200], Ma U[0.1,0.8], "
                        "seeded phases (seed 0), 8th order, Wray RK3, FP32 RHS / FP64 state"}
+    # the other execution mode on the same members
+    other = 1 - mode
+    bt.set_mode(other)
+    if other == 0:
+        bt.set_shape(128, 4)
+    oms, _ = timed()
+    out["other_mode"] = {"mode": names[other], "value": pts * args.steps / (oms * 1e-3) / 1e6,
+                         "ms_per_step": oms / args.steps}
+    if other == 0:
+        out["other_mode"]["launch_shape"] = {"threads": 128, "blocks_per_sm": bt.shape()[1]}
     bt.close()
     return out
 

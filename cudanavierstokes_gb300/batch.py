@@ -93,6 +93,16 @@ class Batch:
         native.check(native.lib().cns_batch_get_shape(self._b, ctypes.byref(t), ctypes.byref(b)))
         return t.value, b.value
 
+    def set_mode(self, mode: int) -> None:
+        """0: one persistent launch per RK stage over all members; 1: members' own step
+        graphs on concurrent streams."""
+        native.check(native.lib().cns_batch_set_mode(self._b, int(mode)))
+
+    def mode(self) -> int:
+        m = ctypes.c_int()
+        native.check(native.lib().cns_batch_get_mode(self._b, ctypes.byref(m)))
+        return m.value
+
     def tune(self, steps: int = 2) -> float:
         ms = ctypes.c_double()
         native.check(native.lib().cns_batch_tune(self._b, int(steps), ctypes.byref(ms)))

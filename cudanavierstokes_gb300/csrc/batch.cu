@@ -1,6 +1,11 @@
-// batch.cu -- batched ensemble: many simulations of uneven grid sizes advanced together,
-// one persistent cooperative launch per Runge-Kutta stage, the step captured in a CUDA
-// graph (one per ping-pong parity), launch shape picked by a measuring autotuner.
+// batch.cu -- batched ensemble: many simulations of uneven grid sizes advanced together.
+// Two execution modes, picked with the launch shape by a measuring autotuner:
+//  - persistent: one persistent cooperative launch per Runge-Kutta stage over the work
+//    units of all members, the step captured in a CUDA graph (one per ping-pong parity);
+//  - concurrent: every member advances through its own captured step graph (the
+//    standalone stage kernels, coefficients in the launch parameters) on one of up to
+//    CNS_BATCH_LANES streams forked from and joined into the batch stream, so the
+//    kernels of different members overlap on the device.
 //
 // Each member is a solver handle (own buffers, scalars and logs); the batch keeps a
 // device table of the members' pointers and geometry (BatchInst) and the prefix offsets of
@@ -46,9 +51,10 @@ struct Member {
     int64_t cap = 0;        // per-step log capacity
 };
 
-// launch shapes chosen by the autotuner, keyed by precision, stencil orders and a size class
+// execution modes and launch shapes chosen by the autotuner, keyed by precision, stencil
+// orders and a size class
 std::mutex g_tune_mu;
-std::map<std::tuple<int, int, int, int>, std::pair<int, int>> g_tuned;
+std::map<std::tuple<int, int, int, int>, std::tuple<int, int, int>> g_tuned;   // -> mode, threads, blocks/SM
 
 int size_class(int64_t points) {
     int c = 0;
@@ -83,6 +89,10 @@ struct cns_batch {
     bool tuned = false;
     cudaGraphExec_t exec[2] = {nullptr, nullptr};
     int64_t launches = 0;
+    int mode = CNS_BATCH_PERSISTENT;
+    std::vector<cudaStream_t> lanes;     // concurrent mode
+    std::vector<cudaEvent_t> lane_done;
+    cudaEvent_t fork = nullptr;
 
     void drop_graphs() {
         for (int c = 0; c < 2; c++)
@@ -96,6 +106,9 @@ struct cns_batch {
         if (d_ctl) cudaFree(d_ctl);
         if (d_bar) cudaFree(d_bar);
         if (d_err) cudaFree(d_err);
+        for (auto s : lanes) cudaStreamDestroy(s);
+        for (auto e : lane_done) cudaEventDestroy(e);
+        if (fork) cudaEventDestroy(fork);
         if (own_stream) cudaStreamDestroy(own_stream);
     }
 };
@@ -223,6 +236,41 @@ int step_stages(cns_batch* b) {
     BCK(cudaGraphLaunch(b->exec[c], b->stream));
     b->launches += 3;
     b->cur = c ^ 1;   // three stages: parity flips once per step
+    return CNS_OK;
+}
+
+// concurrent mode: one step of every member through its own step graph, members spread
+// over the lanes (fork from the batch stream, join back into it)
+int step_members(cns_batch* b) {
+    const int n = (int)b->members.size();
+    const int K = std::min(n, CNS_BATCH_LANES);
+    while ((int)b->lanes.size() < K) {
+        cudaStream_t s = nullptr;
+        cudaEvent_t e = nullptr;
+        BCK(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
+        b->lanes.push_back(s);
+        BCK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+        b->lane_done.push_back(e);
+    }
+    if (!b->fork) BCK(cudaEventCreateWithFlags(&b->fork, cudaEventDisableTiming));
+    BCK(cudaEventRecord(b->fork, b->stream));
+    for (int k = 0; k < K; k++) BCK(cudaStreamWaitEvent(b->lanes[k], b->fork, 0));
+    int rc = CNS_OK;
+    for (int q = 0; q < n && !rc; q++) {
+        cns_solver* h = b->members[q].h;
+        h->stream = b->lanes[q % K];
+        h->cur = b->cur;
+        const int64_t l0 = h->launches;
+        rc = cns::solver_step(h);
+        b->launches += h->launches - l0;
+        h->stream = b->stream;
+    }
+    for (int k = 0; k < K; k++) {   // join even after an error, so no lane work is left behind
+        BCK(cudaEventRecord(b->lane_done[k], b->lanes[k]));
+        BCK(cudaStreamWaitEvent(b->stream, b->lane_done[k], 0));
+    }
+    if (rc) return rc;
+    b->cur ^= 1;   // three stages: parity flips once per step
     return CNS_OK;
 }
 
@@ -433,7 +481,7 @@ int cns_batch_step(cns_batch* b, int nsteps) {
             }
             if (want && (rc = cns::solver_reduce(h, want, dg))) return rc;
         }
-        if ((rc = step_stages(b))) return rc;
+        if ((rc = b->mode == CNS_BATCH_CONCURRENT ? step_members(b) : step_stages(b))) return rc;
         for (auto& m : b->members) m.steps++;
     }
     BCK(cudaStreamSynchronize(b->stream));
@@ -468,6 +516,19 @@ int cns_batch_set_shape(cns_batch* b, int threads, int blocks_per_sm) {
     return CNS_OK;
 }
 
+int cns_batch_set_mode(cns_batch* b, int mode) {
+    if (!b || (mode != CNS_BATCH_PERSISTENT && mode != CNS_BATCH_CONCURRENT))
+        return cns::set_error(CNS_ERR_INVALID, "mode must be CNS_BATCH_PERSISTENT or CNS_BATCH_CONCURRENT");
+    b->mode = mode;
+    return CNS_OK;
+}
+
+int cns_batch_get_mode(cns_batch* b, int* mode) {
+    if (!b || !mode) return cns::set_error(CNS_ERR_INVALID, "NULL argument");
+    *mode = b->mode;
+    return CNS_OK;
+}
+
 int cns_batch_get_shape(cns_batch* b, int* threads, int* blocks_per_sm) {
     if (!b) return cns::set_error(CNS_ERR_INVALID, "batch is NULL");
     if (threads) *threads = b->threads;
@@ -475,9 +536,9 @@ int cns_batch_get_shape(cns_batch* b, int* threads, int* blocks_per_sm) {
     return CNS_OK;
 }
 
-// Measure each launch shape on the current members (advancing them by `steps` steps per
-// candidate) and keep the fastest; results are cached per precision, stencil orders and
-// size class for later batches.
+// Measure each execution mode and launch shape on the current members (advancing them by
+// `steps` steps per candidate) and keep the fastest; results are cached per precision,
+// stencil orders and size class for later batches.
 int cns_batch_tune(cns_batch* b, int steps, double* best_ms) {
     if (!b || steps < 1) return cns::set_error(CNS_ERR_INVALID, "bad arguments");
     if (b->members.empty()) return cns::set_error(CNS_ERR_STATE, "tune needs members");
@@ -489,7 +550,8 @@ int cns_batch_tune(cns_batch* b, int steps, double* best_ms) {
         auto it = g_tuned.find(key);
         if (it != g_tuned.end()) {
             if (best_ms) *best_ms = -1.0;
-            return cns_batch_set_shape(b, it->second.first, it->second.second);
+            int rc = cns_batch_set_mode(b, std::get<0>(it->second));
+            return rc ? rc : cns_batch_set_shape(b, std::get<1>(it->second), std::get<2>(it->second));
         }
     }
     BCK(cudaSetDevice(b->device));
@@ -497,31 +559,38 @@ int cns_batch_tune(cns_batch* b, int steps, double* best_ms) {
     BCK(cudaEventCreate(&e0));
     BCK(cudaEventCreate(&e1));
     double best = 1e30;
-    int bt = b->threads, bb = b->blocks_per_sm;
+    int bm = b->mode, bt = b->threads, bb = b->blocks_per_sm;
+    auto measure = [&](int mode, int threads, int bps) -> int {
+        int rc = cns_batch_set_mode(b, mode);
+        if (!rc && mode == CNS_BATCH_PERSISTENT) rc = cns_batch_set_shape(b, threads, bps);
+        if (rc) return CNS_OK;   // shape not available: skip the candidate
+        if ((rc = cns_batch_step(b, 1))) return rc;   // capture + warm-up
+        BCK(cudaEventRecord(e0, b->stream));
+        if ((rc = cns_batch_step(b, steps))) return rc;
+        BCK(cudaEventRecord(e1, b->stream));
+        BCK(cudaEventSynchronize(e1));
+        float ms = 0.f;
+        BCK(cudaEventElapsedTime(&ms, e0, e1));
+        if (ms < best) { best = ms; bm = mode; bt = b->threads; bb = b->blocks_per_sm; }
+        return CNS_OK;
+    };
+    int rc = measure(CNS_BATCH_CONCURRENT, b->threads, b->blocks_per_sm);
     for (int threads : {128, 256}) {
         int occ = 0;
-        if (batch_stage_occupancy(b->precision == CNS_PREC_FP32_RHS, b->S, b->V, threads, &occ) || occ < 1) continue;
-        for (int bps = 1; bps <= std::min(occ, 4); bps++) {
-            int rc = cns_batch_set_shape(b, threads, bps);
-            if (rc) continue;
-            if ((rc = cns_batch_step(b, 1))) return rc;   // capture + warm-up
-            BCK(cudaEventRecord(e0, b->stream));
-            if ((rc = cns_batch_step(b, steps))) return rc;
-            BCK(cudaEventRecord(e1, b->stream));
-            BCK(cudaEventSynchronize(e1));
-            float ms = 0.f;
-            BCK(cudaEventElapsedTime(&ms, e0, e1));
-            if (ms < best) { best = ms; bt = threads; bb = bps; }
-        }
+        if (rc || batch_stage_occupancy(b->precision == CNS_PREC_FP32_RHS, b->S, b->V, threads, &occ) || occ < 1)
+            continue;
+        for (int bps = 1; bps <= std::min(occ, 4) && !rc; bps++) rc = measure(CNS_BATCH_PERSISTENT, threads, bps);
     }
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
+    if (rc) return rc;
     {
         std::lock_guard<std::mutex> lk(g_tune_mu);
-        g_tuned[key] = {bt, bb};
+        g_tuned[key] = std::make_tuple(bm, bt, bb);
     }
     if (best_ms) *best_ms = best / steps;
-    return cns_batch_set_shape(b, bt, bb);
+    rc = cns_batch_set_mode(b, bm);
+    return rc ? rc : cns_batch_set_shape(b, bt, bb);
 }
 
 // Failure-detection self test of the bounded grid barrier: a one-block launch waits for a

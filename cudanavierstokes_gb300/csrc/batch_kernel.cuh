@@ -100,7 +100,7 @@ __global__ void __launch_bounds__(256, sizeof(R) == 4 ? 2 : 1) k_batch_stage(con
         const int bx = (int)(lu % I.nbx), by = (int)((lu / I.nbx) % I.nby), k = (int)(lu / ((long long)I.nbx * I.nby));
         const int i = bx * 32 + tx, j = by * rows + ty;
         if (stage0 && lu == 0 && threadIdx.x == 0)
-            advance_time(I.scal, (long long)I.scal[SC_STEP] < I.tcap ? I.tlog : nullptr);
+            advance_time(I.scal, I.tlog, I.tcap);
         if (i < I.g.mx && j < I.g.my) {
             DerivedOut<R> o{I.der[0], I.der[1], I.der[2], I.der[3], I.s32[0], I.s32[1], I.s32[2], I.s32[3]};
             state_point<R>(I.g, I.ph, StateIn{I.q[cur][0], I.q[cur][1], I.q[cur][2], I.q[cur][3], I.q[cur][4]}, o,

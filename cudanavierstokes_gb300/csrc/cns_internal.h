@@ -74,7 +74,7 @@ struct Update {
 
 template <typename R>
 void launch_state(const Geom& g, const Phys& ph, const StateIn& q, const DerivedOut<R>& o, double* scal,
-                  int advance_time, double* time_log, cudaStream_t s);
+                  int advance_time, double* time_log, long long tcap, cudaStream_t s);
 template <typename R>
 void launch_ghost_state(const Geom& g, const Phys& ph, const StencilFields<R>& f, const double* scal, cudaStream_t s);
 template <typename R>

@@ -9,11 +9,11 @@ namespace cns {
 // Single-solver kernels: thin grids over the per-point bodies of kernels_point.cuh.
 template <typename R>
 __global__ void __launch_bounds__(128) k_state(Geom g, Phys ph, StateIn q, DerivedOut<R> o, double* scal,
-                                               int adv, double* time_log) {
+                                               int adv, double* time_log, long long tcap) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     const int j = blockIdx.y * blockDim.y + threadIdx.y;
     const int k = blockIdx.z;
-    if (adv && i == 0 && j == 0 && k == 0) advance_time(scal, time_log);
+    if (adv && i == 0 && j == 0 && k == 0) advance_time(scal, time_log, tcap);
     if (i >= g.mx || j >= g.my) return;
     state_point<R>(g, ph, q, o, scal, i, j, k);
 }
@@ -179,8 +179,8 @@ static inline unsigned ghost_blocks(const Geom& g) { return (unsigned)((ghost_co
 
 template <typename R>
 void launch_state(const Geom& g, const Phys& ph, const StateIn& q, const DerivedOut<R>& o, double* scal,
-                  int advance_time, double* time_log, cudaStream_t s) {
-    k_state<R><<<point_grid(g), point_block(), 0, s>>>(g, ph, q, o, scal, advance_time, time_log);
+                  int advance_time, double* time_log, long long tcap, cudaStream_t s) {
+    k_state<R><<<point_grid(g), point_block(), 0, s>>>(g, ph, q, o, scal, advance_time, time_log, tcap);
 }
 template <typename R>
 void launch_ghost_state(const Geom& g, const Phys& ph, const StencilFields<R>& f, const double* scal, cudaStream_t s) {
@@ -221,7 +221,7 @@ void launch_pack(const Geom& g, const T* src, double* dst, cudaStream_t s) {
 
 #define CNS_INST(R)                                                                                               \
     template void launch_state<R>(const Geom&, const Phys&, const StateIn&, const DerivedOut<R>&, double*, int,   \
-                                  double*, cudaStream_t);                                                        \
+                                  double*, long long, cudaStream_t);                                                        \
     template void launch_ghost_state<R>(const Geom&, const Phys&, const StencilFields<R>&, const double*,          \
                                         cudaStream_t);                                                           \
     template void launch_ghost_scalar<R>(const Geom&, R*, cudaStream_t);                                          \

@@ -45,14 +45,17 @@ __device__ __forceinline__ void state_point(const Geom& g, const Phys& ph, const
 }
 
 // Stage 0 of a step advances the simulation time by dt (deviceAdvanceTime) and, with a
-// time log, stores the new time at the device step counter and advances the counter.
-__device__ __forceinline__ void advance_time(double* scal, double* time_log) {
+// time log of capacity tcap, stores the new time at the device step counter and advances
+// the counter (a full log is left as it is).
+__device__ __forceinline__ void advance_time(double* scal, double* time_log, long long tcap) {
     const double tn = scal[SC_TIME] + scal[SC_DT];
     scal[SC_TIME] = tn;
     if (time_log) {
         const long long st = (long long)scal[SC_STEP];
-        time_log[st] = tn;
-        scal[SC_STEP] = (double)(st + 1);
+        if (st < tcap) {
+            time_log[st] = tn;
+            scal[SC_STEP] = (double)(st + 1);
+        }
     }
 }
 

@@ -3,8 +3,9 @@
 // Clients submit (parameters, initial fields, N) from any thread. One worker thread owns
 // the GPU batch: between steps it admits queued requests in arrival order while the HBM
 // budget allows (cns_batch_add fails with CNS_ERR_OOM otherwise and the request waits),
-// advances every resident simulation by one step (one persistent launch per RK stage for
-// all of them), and retires the ones that reached their N: their fields are copied to host
+// advances every resident simulation by one step (the batch's concurrent mode: each
+// member's step graph on one of the batch's streams, so their kernels overlap), and
+// retires the ones that reached their N: their fields are copied to host
 // memory, their device memory is released and their latency (submit -> result ready) is
 // recorded. State stays on the device for the whole life of a request.
 #include <algorithm>
@@ -173,6 +174,7 @@ int cns_server_create(int device, int precision, int stencil_size, int stencil_v
     cns_batch* b = nullptr;
     int rc = cns_batch_create(device, precision, stencil_size, stencil_visc, hbm_budget_bytes, &b);
     if (rc) return rc;
+    cns_batch_set_mode(b, CNS_BATCH_CONCURRENT);
     cns_server* s = new cns_server();
     s->batch = b;
     s->device = device;

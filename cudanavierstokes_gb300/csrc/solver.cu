@@ -126,7 +126,8 @@ int state_phase(cns_solver* h, int advance_time, double* time_log) {
         f.r = (R*)h->q[h->cur][0]; f.u = (R*)h->q[h->cur][1]; f.v = (R*)h->q[h->cur][2]; f.w = (R*)h->q[h->cur][3];
     }
     f.t = o.t; f.p = o.p; f.h = o.h; f.m = o.m;
-    launch_state<R>(h->geom, h->phys, state_in(h, h->cur), o, h->scal, advance_time, time_log, h->stream);
+    launch_state<R>(h->geom, h->phys, state_in(h, h->cur), o, h->scal, advance_time, time_log, h->diag_cap,
+                    h->stream);
     launch_ghost_state<R>(h->geom, h->phys, f, h->scal, h->stream);
     h->launches += 2;
     CKL();
@@ -255,6 +256,12 @@ int step_graph(cns_solver* h) {
     h->cur = c ^ (nst & 1);
     return CNS_OK;
 }
+
+}  // namespace
+
+int cns::solver_step(cns_solver* h) { return h->use_graphs ? step_graph(h) : step_stages(h, h->tlog); }
+
+namespace {
 
 int upload_grid_tables(cns_solver* h) {
     const int mx = h->p.mx, V = h->p.stencil_visc;

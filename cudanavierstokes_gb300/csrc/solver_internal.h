@@ -115,4 +115,7 @@ inline void solver_set_parity(cns_solver* h, int want) {
     h->drop_graphs();
 }
 int solver_reduce(cns_solver* h, int want, double* diag);
+// one time step of the handle's scheme on h->stream (through its step graph when graphs
+// are on), logging the time at the device step counter up to diag_cap entries
+int solver_step(cns_solver* h);
 }  // namespace cns

@@ -54,6 +54,8 @@ SIGNATURES = {
     "cns_batch_step": (ctypes.c_int, [_vp, ctypes.c_int]),
     "cns_batch_set_shape": (ctypes.c_int, [_vp, ctypes.c_int, ctypes.c_int]),
     "cns_batch_get_shape": (ctypes.c_int, [_vp, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int)]),
+    "cns_batch_set_mode": (ctypes.c_int, [_vp, ctypes.c_int]),
+    "cns_batch_get_mode": (ctypes.c_int, [_vp, ctypes.POINTER(ctypes.c_int)]),
     "cns_batch_tune": (ctypes.c_int, [_vp, ctypes.c_int, _dp]),
     "cns_selftest_barrier_timeout": (ctypes.c_int, [ctypes.c_int, ctypes.c_longlong, ctypes.POINTER(ctypes.c_int)]),
     "cns_probe_fma_peak": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, ctypes.c_int, _dp]),

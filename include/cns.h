@@ -271,6 +271,17 @@ CNS_API int cns_batch_step(cns_batch* b, int nsteps);
  * (clamped to the co-residency limit). */
 CNS_API int cns_batch_set_shape(cns_batch* b, int threads, int blocks_per_sm);
 CNS_API int cns_batch_get_shape(cns_batch* b, int* threads, int* blocks_per_sm);
+
+/* Execution mode (no counterpart in the reference): CNS_BATCH_PERSISTENT advances all
+ * members with one persistent cooperative launch per RK stage (launch shape as above);
+ * CNS_BATCH_CONCURRENT advances each member through its own captured step graph on one
+ * of up to CNS_BATCH_LANES streams, so the members' kernels overlap. cns_batch_tune
+ * measures both and keeps the faster. */
+#define CNS_BATCH_PERSISTENT 0
+#define CNS_BATCH_CONCURRENT 1
+#define CNS_BATCH_LANES 16
+CNS_API int cns_batch_set_mode(cns_batch* b, int mode);
+CNS_API int cns_batch_get_mode(cns_batch* b, int* mode);
 /* Autotune the launch shape by timing `steps` steps per candidate on the current members
  * (the members advance); the choice is cached per precision, stencil orders and size
  * class. best_ms receives the best time per step (-1 when taken from the cache). */

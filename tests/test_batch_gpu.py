@@ -1,6 +1,7 @@
-"""Batched ensemble (one persistent launch per RK stage for all members): members of uneven
-size and physics against standalone solvers; a member's result is identical alone and in a
-mix; membership changes between steps; the autotuner; the bounded barrier's give-up path."""
+"""Batched ensemble, in both execution modes (one persistent launch per RK stage for all
+members; members' own step graphs on concurrent streams): members of uneven size and
+physics against standalone solvers; a member's result is identical alone and in a mix;
+membership changes between steps; the autotuner; the bounded barrier's give-up path."""
 import ctypes
 
 import numpy as np
@@ -25,11 +26,16 @@ def members(prec):
     return [(a, fa), (b, fb), (c, fc)]
 
 
+MODES = (0, 1)   # persistent, concurrent
+
+
+@pytest.mark.parametrize("mode", MODES)
 @pytest.mark.parametrize("prec", [PREC_FP64, PREC_FP32_RHS])
-def test_batch_matches_standalone_solvers(gpu_lib, prec):
+def test_batch_matches_standalone_solvers(gpu_lib, prec, mode):
     ms = members(prec)
     n = 5
     bt = Batch(precision=prec)
+    bt.set_mode(mode)
     ids = [bt.add(p, f, max_steps=16) for p, f in ms]
     bt.step(n)
     tol = 1e-12 if prec == PREC_FP64 else 1e-6
@@ -46,21 +52,26 @@ def test_batch_matches_standalone_solvers(gpu_lib, prec):
         assert bt.steps_done(mid) == n
 
 
-def test_member_alone_equals_member_in_mix(gpu_lib):
+@pytest.mark.parametrize("mode", MODES)
+def test_member_alone_equals_member_in_mix(gpu_lib, mode):
     ms = members(PREC_FP32_RHS)
     alone = Batch(precision=PREC_FP32_RHS)
+    alone.set_mode(mode)
     i0 = alone.add(*ms[1], max_steps=8)
     alone.step(4)
     mix = Batch(precision=PREC_FP32_RHS)
+    mix.set_mode(mode)
     ids = [mix.add(p, f, max_steps=8) for p, f in ms]
     mix.step(4)
     for a, b in zip(alone.fields(i0), mix.fields(ids[1])):
         assert np.array_equal(a, b)
 
 
-def test_membership_changes_between_steps(gpu_lib):
+@pytest.mark.parametrize("mode", MODES)
+def test_membership_changes_between_steps(gpu_lib, mode):
     ms = members(PREC_FP64)
     bt = Batch(precision=PREC_FP64)
+    bt.set_mode(mode)
     i0 = bt.add(*ms[0], max_steps=20)
     bt.step(2)
     i1 = bt.add(*ms[1], max_steps=20)     # joins later (other ping-pong parity)
@@ -94,6 +105,7 @@ def test_autotune_and_shapes(gpu_lib):
     ms_best = bt.tune(2)
     t, b = bt.shape()
     assert t in (128, 256) and b >= 1
+    assert bt.mode() in MODES
     assert ms_best > 0 or ms_best == -1.0
     bt.step(1)
 
