@@ -150,22 +150,43 @@ __global__ void __launch_bounds__(256, sizeof(R) == 4 ? 2 : 1) k_batch_stage(con
         if (t < ghost_count(I.g)) ghost_scalar_cell<R>(I.g, I.dil, t);
     }
     grid_barrier(bar, nb, err);
-    // phase 5: RHS + stage update into the other state buffer
+    // phase 5: RHS + stage update into the other state buffer. The unit's x-y neighbourhood
+    // of the nine stencil fields is staged in shared memory (as in the tiled single-solver
+    // kernel); z neighbours come from global memory.
+    constexpr int TX = 32 + 2 * S, FSMAX = TX * (8 + 2 * S);
+    __shared__ R tile[TF_COUNT * FSMAX];
+    const int FS = TX * (rows + 2 * S), nt = blockDim.x;
     for (long long u = blockIdx.x; u < npu; u += gridDim.x) {
         const int q = find_inst(ctl->unit_off, n, u);
         const BatchInst<R>& I = tab[q];
         const long long lu = u - ctl->unit_off[q];
         const int bx = (int)(lu % I.nbx), by = (int)((lu / I.nbx) % I.nby), k = (int)(lu / ((long long)I.nbx * I.nby));
-        const int i = bx * 32 + tx, j = by * rows + ty;
-        if (i < I.g.mx && j < I.g.my) {
-            RhsIn<R> in;
-            if (I.s32[0]) { in.r = I.s32[0]; in.u = I.s32[1]; in.v = I.s32[2]; in.w = I.s32[3]; }
-            else {
-                in.r = (const R*)I.q[cur][0]; in.u = (const R*)I.q[cur][1];
-                in.v = (const R*)I.q[cur][2]; in.w = (const R*)I.q[cur][3];
+        const int i0 = bx * 32, j0 = by * rows;
+        RhsIn<R> in;
+        if (I.s32[0]) { in.r = I.s32[0]; in.u = I.s32[1]; in.v = I.s32[2]; in.w = I.s32[3]; }
+        else {
+            in.r = (const R*)I.q[cur][0]; in.u = (const R*)I.q[cur][1];
+            in.v = (const R*)I.q[cur][2]; in.w = (const R*)I.q[cur][3];
+        }
+        in.h = I.der[0]; in.t = I.der[1]; in.p = I.der[2]; in.m = I.der[3]; in.dil = I.dil;
+        for (int c = 0; c < 9; c++) in.g[c] = I.grad[c];
+        __syncthreads();   // the previous unit is done with the tile
+        {
+            const long long org = I.g.at(i0 - S, j0 - S, k);
+            const int xlim = I.g.mx + 2 * S - i0, ylim = I.g.my + 2 * S - j0;
+            const long long P = I.g.P;
+            const R* src[TF_COUNT] = {in.u, in.v, in.w, in.r, in.h, in.p, in.t, in.m, in.dil};
+#pragma unroll
+            for (int f = 0; f < TF_COUNT; f++) {
+                for (int e = threadIdx.x; e < FS; e += nt) {
+                    const int yy = e / TX, xx = e - yy * TX;
+                    tile[f * FS + e] = (xx < xlim && yy < ylim) ? ld(src[f], org + (long long)yy * P + xx) : (R)0;
+                }
             }
-            in.h = I.der[0]; in.t = I.der[1]; in.p = I.der[2]; in.m = I.der[3]; in.dil = I.dil;
-            for (int c = 0; c < 9; c++) in.g[c] = I.grad[c];
+        }
+        __syncthreads();
+        const int i = i0 + tx, j = j0 + ty;
+        if (i < I.g.mx && j < I.g.my) {
             Update<R> up;
             up.kind = kind; up.a = a; up.b = b; up.ca = (R)a; up.cb = (R)b; up.use_prev = a != 0.0;
             up.qin = StateIn{I.q[cur][0], I.q[cur][1], I.q[cur][2], I.q[cur][3], I.q[cur][4]};
@@ -174,7 +195,13 @@ __global__ void __launch_bounds__(256, sizeof(R) == 4 ? 2 : 1) k_batch_stage(con
             for (int c = 0; c < 5; c++) { up.rb[c] = I.rb[c]; up.k2[c] = nullptr; up.q0[c] = nullptr; }
             up.spx = I.spx; up.spz = I.spz; up.rref = I.rref; up.uref = I.uref; up.vref = I.vref;
             up.wref = I.wref; up.eref = I.eref;
-            rhs_point<R, S, V>(I.g, I.cf, in, up, I.scal, quirk, i, j, k);
+            const R* ctr = tile + (ty + S) * TX + (tx + S);
+            const NbTile<R> nbx{ctr, 1, FS}, nby{ctr, TX, FS};
+            const long long c = I.g.at(i, j, k);
+            const NbGlobal<R> nbz{&in, c, I.g.PS};
+            rhs_point_nb<R, S, V>(I.g, I.cf, in, up, I.scal, quirk, i, k, c, nbx, nby, nbz, ctr[TF_DIL * FS],
+                                  ctr[TF_M * FS], ctr[TF_U * FS], ctr[TF_V * FS], ctr[TF_W * FS], ctr[TF_R * FS],
+                                  ctr[TF_H * FS]);
         }
     }
 }

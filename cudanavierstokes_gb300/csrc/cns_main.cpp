@@ -9,7 +9,8 @@
 // checkCFLcondition, checkBulk, Re, Pr, Ma, viscexp, gam, stretch, TwallTop, TwallBot) plus
 // optional precision (0 FP64, 1 FP32 RHS) and quirk_dissipation_y. Output as the reference:
 // fields/{x,y,z}.bin, Grid.txt, fields/{r,u,v,w,e}.%07d.bin (raw FP64, [k][j][i]),
-// solution.txt ("step time kin par2 dtime" every checkCFLcondition steps). A boundary layer
+// solution.txt ("step time kin par2 dtime" every checkCFLcondition steps), and an XDMF
+// descriptor fields/fields.xmf of the files this run wrote. A boundary layer
 // reads blasius1D/{x,r,u,w,e}Prof.bin. Without restart the initial field is the reference's
 // own: initChannel (forcing), initCHIT (periodic box) or the sponge reference fields.
 #include <chrono>
@@ -65,6 +66,64 @@ bool read_bin(const std::string& path, std::vector<double>& a) {
     const bool ok = fread(a.data(), sizeof(double), a.size(), f) == a.size();
     fclose(f);
     return ok;
+}
+
+// XDMF 2 descriptor of the written fields (the format python-utils/writexmf.py produces
+// for the reference's output): a 3D rectilinear mesh from x, y, z and a temporal
+// collection with one uniform grid per file index, its r, u, v, w, e attributes read as
+// native-endian FP64 binaries from fields/%c.%07d.bin.
+bool write_xmf(const std::string& path, const std::vector<double>& x, const std::vector<double>& y,
+               const std::vector<double>& z, const std::vector<std::pair<int, double>>& files) {
+    FILE* f = fopen(path.c_str(), "w");
+    if (!f) return false;
+    const char* xml = "Format=\"XML\" DataType=\"Float\" Precision=\"8\"";
+    const char* bin = "Format=\"Binary\" DataType=\"Float\" Precision=\"8\" Endian=\"Native\"";
+    const size_t nx = x.size(), ny = y.size(), nz = z.size();
+    fprintf(f, "<?xml version=\"1.0\" ?>\n<!DOCTYPE Xdmf SYSTEM \"Xdmf.dtd\" []>\n");
+    fprintf(f, "<Xdmf xmlns:xi=\"http://www.w3.org/2001/XInclude\" Version=\"2.0\">\n<Domain>\n");
+    fprintf(f, "    <Topology name=\"TOPO\" TopologyType=\"3DRectMesh\" Dimensions=\"%zu %zu %zu\"/>\n", nz, ny, nx);
+    fprintf(f, "    <Geometry name=\"GEO\" GeometryType=\"VXVYVZ\">\n");
+    for (const auto* a : {&x, &y, &z}) {
+        fprintf(f, "        <DataItem %s Dimensions=\"%zu\">\n", xml, a->size());
+        for (double v : *a) fprintf(f, " %.15e", v);
+        fprintf(f, "\n        </DataItem>\n");
+    }
+    fprintf(f, "    </Geometry>\n");
+    fprintf(f, "    <Grid Name=\"TimeSeries\" GridType=\"Collection\" CollectionType=\"Temporal\">\n");
+    fprintf(f, "        <Time TimeType=\"List\">\n            <DataItem %s Dimensions=\"%zu\">\n", xml, files.size());
+    for (const auto& t : files) fprintf(f, " %.15e", t.second);
+    fprintf(f, "\n            </DataItem>\n        </Time>\n");
+    for (const auto& t : files) {
+        fprintf(f, "        <Grid Name=\"T%07d\" GridType=\"Uniform\">\n", t.first);
+        fprintf(f, "            <Topology Reference=\"/Xdmf/Domain/Topology[1]\"/>\n");
+        fprintf(f, "            <Geometry Reference=\"/Xdmf/Domain/Geometry[1]\"/>\n");
+        for (const char* n : {"r", "u", "v", "w", "e"}) {
+            fprintf(f, "            <Attribute Name=\"%s\" Center=\"Node\">\n", n);
+            fprintf(f, "                <DataItem %s Dimensions=\"%zu %zu %zu\">\n", bin, nz, ny, nx);
+            fprintf(f, "                    %s.%07d.bin\n                </DataItem>\n            </Attribute>\n", n,
+                    t.first);
+        }
+        fprintf(f, "        </Grid>\n");
+    }
+    fprintf(f, "    </Grid>\n</Domain>\n</Xdmf>\n");
+    return fclose(f) == 0;
+}
+
+// time, dt and body force beside each field file, so a restart continues the clock and
+// the forcing controller (the reference restarts both from their initial values)
+std::string scalars_name(const std::string& dir, int step) {
+    char buf[64];
+    snprintf(buf, sizeof buf, "/fields/scalars.%07d.txt", step);
+    return dir + buf;
+}
+
+void write_scalars(cns_solver* h, const std::string& dir, int step) {
+    double dt = 0, dpdz = 0, t = 0;
+    cns_get_scalars(h, &dt, &dpdz, &t);
+    if (FILE* f = fopen(scalars_name(dir, step).c_str(), "w")) {
+        fprintf(f, "time = %.17g\ndt = %.17g\ndpdz = %.17g\n", t, dt, dpdz);
+        fclose(f);
+    }
 }
 
 std::string field_name(const std::string& dir, char c, int step) {
@@ -208,10 +267,23 @@ int main(int argc, char** argv) {
             return 2;
         }
     }
+    if (restart >= 0) {
+        auto sc = read_kv(scalars_name(dir, restart).c_str());
+        if (sc.count("time") && sc.count("dt") && sc.count("dpdz"))
+            cns_set_scalars(h, std::strtod(sc["dt"].c_str(), nullptr), std::strtod(sc["dpdz"].c_str(), nullptr),
+                            std::strtod(sc["time"].c_str(), nullptr), -1);
+    }
+    std::vector<std::pair<int, double>> written;
+    {
+        double t0 = 0;
+        cns_get_scalars(h, nullptr, nullptr, &t0);
+        written.push_back({restart < 0 ? 0 : restart, t0});
+    }
     if (restart < 0) {
         cns_copy_field(h, 1, f[0].data(), f[1].data(), f[2].data(), f[3].data(), f[4].data());
         const char* names = "ruvwe";
         for (int q = 0; q < 5; q++) write_bin(field_name(dir, names[q], 0), f[q].data(), N);
+        write_scalars(h, dir, 0);
     }
 
     // solverWrapper (src/cuda_main.cu:267-324)
@@ -229,6 +301,8 @@ int main(int argc, char** argv) {
         cns_copy_field(h, 1, f[0].data(), f[1].data(), f[2].data(), f[3].data(), f[4].data());
         const char* names = "ruvwe";
         for (int q = 0; q < 5; q++) write_bin(field_name(dir, names[q], file), f[q].data(), N);
+        write_scalars(h, dir, file);
+        written.push_back({file, tim[nsteps - 1]});
         printf("file number: %d  \t step: %d  \t time: %lf  \t kin: %le  \t energy: %le\n", file, file * nsteps,
                tim[nsteps - 1], par1[0], par2[0]);
         if (sol)
@@ -238,6 +312,7 @@ int main(int argc, char** argv) {
         tprev = tim[nsteps - 1];
     }
     if (sol) fclose(sol);
+    write_xmf(dir + "/fields/fields.xmf", x, y, z, written);
     cns_destroy(h);
     const double total = std::chrono::duration<double>(std::chrono::steady_clock::now() - t_begin).count();
     printf("The total time is: %g\n", total);

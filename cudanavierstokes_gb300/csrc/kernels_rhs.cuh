@@ -20,33 +20,74 @@
 #include "cns_common.cuh"
 #include "cns_internal.h"
 
+#ifndef CNS_RHS_TILE_ROWS
+#define CNS_RHS_TILE_ROWS 4   // rows of a tiled RHS block (32 x rows threads)
+#endif
+
 namespace cns {
 
 template <typename R>
 __device__ __forceinline__ R ld(const R* __restrict__ p, long long o) { return __ldg(p + o); }
 
-template <typename R, int K>
-__device__ __forceinline__ R d1(const R* __restrict__ f, long long c, long long st, const R* co) {
-    R s = co[1] * (ld(f, c + st) - ld(f, c - st));
+// Neighbours of the centre point along one direction: in global memory at a stride, or in
+// the shared-memory plane tile of the tiled kernel (fields in the tile order TF_*).
+enum { TF_U, TF_V, TF_W, TF_R, TF_H, TF_P, TF_T, TF_M, TF_DIL, TF_COUNT };
+
+template <typename R>
+struct NbGlobal {
+    const RhsIn<R>* in;
+    long long c, st;
+    __device__ __forceinline__ R u(int l) const { return ld(in->u, c + l * st); }
+    __device__ __forceinline__ R v(int l) const { return ld(in->v, c + l * st); }
+    __device__ __forceinline__ R w(int l) const { return ld(in->w, c + l * st); }
+    __device__ __forceinline__ R r(int l) const { return ld(in->r, c + l * st); }
+    __device__ __forceinline__ R h(int l) const { return ld(in->h, c + l * st); }
+    __device__ __forceinline__ R p(int l) const { return ld(in->p, c + l * st); }
+    __device__ __forceinline__ R t(int l) const { return ld(in->t, c + l * st); }
+    __device__ __forceinline__ R m(int l) const { return ld(in->m, c + l * st); }
+    __device__ __forceinline__ R dil(int l) const { return ld(in->dil, c + l * st); }
+};
+
+template <typename R>
+struct NbTile {
+    const R* ctr;   // the centre point in field 0 of the tile
+    int step, fs;   // neighbour step (1 along x, the tile width along y), field stride
+    __device__ __forceinline__ R at(int f, int l) const { return ctr[f * fs + l * step]; }
+    __device__ __forceinline__ R u(int l) const { return at(TF_U, l); }
+    __device__ __forceinline__ R v(int l) const { return at(TF_V, l); }
+    __device__ __forceinline__ R w(int l) const { return at(TF_W, l); }
+    __device__ __forceinline__ R r(int l) const { return at(TF_R, l); }
+    __device__ __forceinline__ R h(int l) const { return at(TF_H, l); }
+    __device__ __forceinline__ R p(int l) const { return at(TF_P, l); }
+    __device__ __forceinline__ R t(int l) const { return at(TF_T, l); }
+    __device__ __forceinline__ R m(int l) const { return at(TF_M, l); }
+    __device__ __forceinline__ R dil(int l) const { return at(TF_DIL, l); }
+};
+
+// first derivative sum_k co[k] (f_k - f_-k) and second derivative co[0] f_0 +
+// sum_k co[k] (f_k + f_-k) of the values get(l), l = -K..K
+template <typename R, int K, class Get>
+__device__ __forceinline__ R d1(const Get& get, const R* co) {
+    R s = co[1] * (get(1) - get(-1));
 #pragma unroll
-    for (int k = 2; k <= K; k++) s = fma(co[k], ld(f, c + k * st) - ld(f, c - k * st), s);
+    for (int k = 2; k <= K; k++) s = fma(co[k], get(k) - get(-k), s);
     return s;
 }
 
-template <typename R, int K>
-__device__ __forceinline__ R d2u(const R* __restrict__ f, long long c, long long st, const R* co) {
-    R s = co[0] * ld(f, c);
+template <typename R, int K, class Get>
+__device__ __forceinline__ R d2u(const Get& get, const R* co) {
+    R s = co[0] * get(0);
 #pragma unroll
-    for (int k = 1; k <= K; k++) s = fma(co[k], ld(f, c + k * st) + ld(f, c - k * st), s);
+    for (int k = 1; k <= K; k++) s = fma(co[k], get(k) + get(-k), s);
     return s;
 }
 
 // non-uniform x second derivative with the per-point table (derDevSharedV2x, nonUniformX)
-template <typename R, int V>
-__device__ __forceinline__ R d2x_nu(const R* __restrict__ f, long long c, const R* __restrict__ cvsx, int mx, int i) {
+template <typename R, int V, class Get>
+__device__ __forceinline__ R d2x_nu(const Get& get, const R* __restrict__ cvsx, int mx, int i) {
     R s = (R)0;
 #pragma unroll
-    for (int it = 0; it < 2 * V + 1; it++) s = fma(__ldg(cvsx + it * mx + i), ld(f, c + (it - V)), s);
+    for (int it = 0; it < 2 * V + 1; it++) s = fma(__ldg(cvsx + it * mx + i), get(it - V), s);
     return s;
 }
 
@@ -54,11 +95,10 @@ __device__ __forceinline__ R d2x_nu(const R* __restrict__ f, long long c, const 
 // (grad mu . s + mu lap u + mu/3 grad theta) of all directions are summed in W[] and the
 // dissipation / conduction in diss / cond, so the energy equation's u_i W_i work term
 // and the mu multiplications are applied once per point instead of once per direction.
-template <typename R, int S, int V, int DIR>
-__device__ __forceinline__ void rhs_direction(const Geom& g, const CoefT<R>& cf, const RhsIn<R>& in, long long c,
-                                              int i, const R (&Gr)[9], R th0, R m0, R m3, R u0, R v0, R w0,
-                                              R r0, R h0, int quirk, R (&acc)[5], R (&W)[3], R& diss, R& cond) {
-    const long long st = DIR == 0 ? 1LL : (DIR == 1 ? g.P : g.PS);
+template <typename R, int S, int V, int DIR, class NB>
+__device__ __forceinline__ void rhs_direction(const Geom& g, const CoefT<R>& cf, const NB& nb, int i,
+                                              const R (&Gr)[9], R th0, R m0, R m3, R u0, R v0, R w0, R r0, R h0,
+                                              int quirk, R (&acc)[5], R (&W)[3], R& diss, R& cond) {
     const bool nux = (DIR == 0) && g.nonuniform_x;
     const R xpi = nux ? cf.xp[i] : (R)1;
     const R* c1V = cf.c1V[DIR];
@@ -81,12 +121,16 @@ __device__ __forceinline__ void rhs_direction(const Geom& g, const CoefT<R>& cf,
     us[S] = u0; vs[S] = v0; ws[S] = w0;
 #pragma unroll
     for (int l = 1; l <= S; l++) {
-        us[S + l] = ld(in.u, c + l * st); us[S - l] = ld(in.u, c - l * st);
-        vs[S + l] = ld(in.v, c + l * st); vs[S - l] = ld(in.v, c - l * st);
-        ws[S + l] = ld(in.w, c + l * st); ws[S - l] = ld(in.w, c - l * st);
+        us[S + l] = nb.u(l); us[S - l] = nb.u(-l);
+        vs[S + l] = nb.v(l); vs[S - l] = nb.v(-l);
+        ws[S + l] = nb.w(l); ws[S - l] = nb.w(-l);
     }
     // d mu/dx s_{DIR,c} + mu d2 u_c/dx2
-    const R dmu = d1<R, V>(in.m, c, st, c1V) * xpi;
+    const auto gm = [&](int l) { return nb.m(l); };
+    const auto gt = [&](int l) { return nb.t(l); };
+    const auto gd = [&](int l) { return nb.dil(l); };
+    const auto gp = [&](int l) { return nb.p(l); };
+    const R dmu = d1<R, V>(gm, c1V) * xpi;
     R d2uu, d2vv, d2ww, d2tt;
     if (nux) {
         R a = (R)0, b = (R)0, e2 = (R)0;
@@ -98,7 +142,7 @@ __device__ __forceinline__ void rhs_direction(const Geom& g, const CoefT<R>& cf,
             e2 = fma(cw, ws[S + it - V], e2);
         }
         d2uu = a; d2vv = b; d2ww = e2;
-        d2tt = d2x_nu<R, V>(in.t, c, cf.cvsx, g.mx, i);
+        d2tt = d2x_nu<R, V>(gt, cf.cvsx, g.mx, i);
     } else {
         R a = c2V[0] * us[S], b = c2V[0] * vs[S], e2 = c2V[0] * ws[S];
 #pragma unroll
@@ -108,19 +152,19 @@ __device__ __forceinline__ void rhs_direction(const Geom& g, const CoefT<R>& cf,
             e2 = fma(c2V[k], ws[S + k] + ws[S - k], e2);
         }
         d2uu = a; d2vv = b; d2ww = e2;
-        d2tt = d2u<R, V>(in.t, c, st, c2V);
+        d2tt = d2u<R, V>(gt, c2V);
     }
     W[0] = fma(tau[0], dmu, fma(d2uu, m0, W[0]));
     W[1] = fma(tau[1], dmu, fma(d2vv, m0, W[1]));
     W[2] = fma(tau[2], dmu, fma(d2ww, m0, W[2]));
     // heat conduction lambda d2T + dlambda dT = (lambda/mu) (mu d2T + dmu dT); the ratio
     // is applied once per point
-    const R dt = d1<R, V>(in.t, c, st, c1V) * xpi;
+    const R dt = d1<R, V>(gt, c1V) * xpi;
     cond = fma(d2tt, m0, cond);
     cond = fma(dt, dmu, cond);
     // mu/3 d(theta) on the DIR momentum (and its work), pressure gradient
-    const R dth = d1<R, V>(in.dil, c, st, c1V) * xpi;
-    const R dp = d1<R, S>(in.p, c, st, c1S) * xpi;
+    const R dth = d1<R, V>(gd, c1V) * xpi;
+    const R dp = d1<R, S>(gp, c1S) * xpi;
     W[DIR] = fma(m3, dth, W[DIR]);
 
     // split-form convective derivatives, telescoped (see file comment); with a uniform
@@ -138,12 +182,11 @@ __device__ __forceinline__ void rhs_direction(const Geom& g, const CoefT<R>& cf,
     const R* fcb = cf.fc[DIR];
 #pragma unroll
     for (int l = 1; l <= S; l++) {
-        const long long o = l * st;
-        const R rm = ld(in.r, c - o), rp = ld(in.r, c + o);
+        const R rm = nb.r(-l), rp = nb.r(l);
         const R um = us[S - l], up = us[S + l];
         const R vm = vs[S - l], vp = vs[S + l];
         const R wm = ws[S - l], wp = ws[S + l];
-        const R hm = ld(in.h, c - o), hp = ld(in.h, c + o);
+        const R hm = nb.h(-l), hp = nb.h(l);
         const R gm = DIR == 0 ? um : (DIR == 1 ? vm : wm);
         const R gp = DIR == 0 ? up : (DIR == 1 ? vp : wp);
         const R Qm = (rm + r0) * (gm + un);
@@ -173,24 +216,23 @@ __device__ __forceinline__ void rhs_direction(const Geom& g, const CoefT<R>& cf,
     acc[1 + DIR] -= dp;
 }
 
-// RHS + stage update of one interior point (i, j, k)
-template <typename R, int S, int V>
-__device__ __forceinline__ void rhs_point(const Geom& g, const CoefT<R>& cf, const RhsIn<R>& in, const Update<R>& up,
-                                          const double* __restrict__ scal, int quirk, int i, int j, int k) {
-    const long long c = g.at(i, j, k);
-
+// RHS + stage update of one interior point (i, ., k) at element c, with the neighbours
+// along x, y, z from the accessors nx, ny, nz and the centre values given
+template <typename R, int S, int V, class NX, class NY, class NZ>
+__device__ __forceinline__ void rhs_point_nb(const Geom& g, const CoefT<R>& cf, const RhsIn<R>& in,
+                                             const Update<R>& up, const double* __restrict__ scal, int quirk, int i,
+                                             int k, long long c, const NX& nx, const NY& ny, const NZ& nz, R th0,
+                                             R m0, R u0, R v0, R w0, R r0, R h0) {
     R Gr[9];
 #pragma unroll
     for (int q = 0; q < 9; q++) Gr[q] = ld(in.g[q], c);
-    const R th0 = ld(in.dil, c), m0 = ld(in.m, c);
-    const R u0 = ld(in.u, c), v0 = ld(in.v, c), w0 = ld(in.w, c), r0 = ld(in.r, c), h0 = ld(in.h, c);
     const R m3 = m0 * (R)(1.0 / 3.0);
     R acc[5] = {0, 0, 0, 0, 0};
     R W[3] = {0, 0, 0};
     R diss = 0, cond = 0;
-    rhs_direction<R, S, V, 0>(g, cf, in, c, i, Gr, th0, m0, m3, u0, v0, w0, r0, h0, quirk, acc, W, diss, cond);
-    rhs_direction<R, S, V, 1>(g, cf, in, c, i, Gr, th0, m0, m3, u0, v0, w0, r0, h0, quirk, acc, W, diss, cond);
-    rhs_direction<R, S, V, 2>(g, cf, in, c, i, Gr, th0, m0, m3, u0, v0, w0, r0, h0, quirk, acc, W, diss, cond);
+    rhs_direction<R, S, V, 0>(g, cf, nx, i, Gr, th0, m0, m3, u0, v0, w0, r0, h0, quirk, acc, W, diss, cond);
+    rhs_direction<R, S, V, 1>(g, cf, ny, i, Gr, th0, m0, m3, u0, v0, w0, r0, h0, quirk, acc, W, diss, cond);
+    rhs_direction<R, S, V, 2>(g, cf, nz, i, Gr, th0, m0, m3, u0, v0, w0, r0, h0, quirk, acc, W, diss, cond);
     acc[1] += W[0];
     acc[2] += W[1];
     acc[3] += W[2];
@@ -282,6 +324,50 @@ __device__ __forceinline__ void rhs_point(const Geom& g, const CoefT<R>& cf, con
     up.qout.e[c] = qn[4];
 }
 
+// RHS + stage update of one interior point (i, j, k), every neighbour from global memory
+template <typename R, int S, int V>
+__device__ __forceinline__ void rhs_point(const Geom& g, const CoefT<R>& cf, const RhsIn<R>& in, const Update<R>& up,
+                                          const double* __restrict__ scal, int quirk, int i, int j, int k) {
+    const long long c = g.at(i, j, k);
+    const R th0 = ld(in.dil, c), m0 = ld(in.m, c);
+    const R u0 = ld(in.u, c), v0 = ld(in.v, c), w0 = ld(in.w, c), r0 = ld(in.r, c), h0 = ld(in.h, c);
+    const NbGlobal<R> nx{&in, c, 1LL}, ny{&in, c, g.P}, nz{&in, c, g.PS};
+    rhs_point_nb<R, S, V>(g, cf, in, up, scal, quirk, i, k, c, nx, ny, nz, th0, m0, u0, v0, w0, r0, h0);
+}
+
+// The RHS kernel with the x-y neighbourhood of the nine stencil fields staged in shared
+// memory: per block one (32 + 2S) x (BY + 2S) tile per field, filled with coalesced row
+// loads; the x and y derivatives read the tile, the z derivatives global memory. Tile
+// cells beyond the ghost layer (possible in the last block of a row or column) are not
+// read from memory; no thread uses them.
+template <typename R, int S, int V, int BY>
+__global__ void __launch_bounds__(32 * BY, (sizeof(R) == 4 ? 768 : 512) / (32 * BY))
+    k_rhs_tiled(Geom g, CoefT<R> cf, RhsIn<R> in, Update<R> up, const double* __restrict__ scal, int quirk) {
+    constexpr int TX = 32 + 2 * S, TY = BY + 2 * S, FS = TX * TY, NT = 32 * BY;
+    __shared__ R tile[TF_COUNT * FS];
+    const int tx = threadIdx.x, ty = threadIdx.y, tid = ty * 32 + tx;
+    const int i0 = blockIdx.x * 32, j0 = blockIdx.y * BY, k = blockIdx.z;
+    const long long org = g.at(i0 - S, j0 - S, k);
+    const int xlim = g.mx + 2 * S - i0, ylim = g.my + 2 * S - j0;
+    const R* src[TF_COUNT] = {in.u, in.v, in.w, in.r, in.h, in.p, in.t, in.m, in.dil};
+#pragma unroll
+    for (int f = 0; f < TF_COUNT; f++) {
+        for (int e = tid; e < FS; e += NT) {
+            const int yy = e / TX, xx = e - yy * TX;
+            tile[f * FS + e] = (xx < xlim && yy < ylim) ? ld(src[f], org + (long long)yy * g.P + xx) : (R)0;
+        }
+    }
+    __syncthreads();
+    const int i = i0 + tx, j = j0 + ty;
+    if (i >= g.mx || j >= g.my) return;
+    const R* ctr = tile + (ty + S) * TX + (tx + S);
+    const NbTile<R> nx{ctr, 1, FS}, ny{ctr, TX, FS};
+    const long long c = g.at(i, j, k);
+    const NbGlobal<R> nz{&in, c, g.PS};
+    rhs_point_nb<R, S, V>(g, cf, in, up, scal, quirk, i, k, c, nx, ny, nz, ctr[TF_DIL * FS], ctr[TF_M * FS],
+                          ctr[TF_U * FS], ctr[TF_V * FS], ctr[TF_W * FS], ctr[TF_R * FS], ctr[TF_H * FS]);
+}
+
 template <typename R, int S, int V>
 __global__ void __launch_bounds__(128, sizeof(R) == 4 ? 6 : 4) k_rhs(Geom g, CoefT<R> cf, RhsIn<R> in, Update<R> up,
                                              const double* __restrict__ scal, int quirk) {
@@ -294,9 +380,19 @@ __global__ void __launch_bounds__(128, sizeof(R) == 4 ? 6 : 4) k_rhs(Geom g, Coe
 template <typename R>
 void launch_rhs_t(int S, int V, const Geom& g, const CoefT<R>& cf, const RhsIn<R>& in, const Update<R>& up,
                   const double* scal, int quirk, cudaStream_t s) {
+    // FP32: the shared-memory tiled kernel (latency-bound on neighbour loads otherwise);
+    // FP64: the FP64 pipe bounds the kernel, neighbours come through L1
+    constexpr int BY = CNS_RHS_TILE_ROWS;
     dim3 grid((g.mx + 31) / 32, (g.my + 3) / 4, g.mz), block(32, 4, 1);
-#define CNS_RHS_CASE(SS, VV) \
-    if (S == SS && V == VV) { k_rhs<R, SS, VV><<<grid, block, 0, s>>>(g, cf, in, up, scal, quirk); return; }
+    dim3 tgrid((g.mx + 31) / 32, (g.my + BY - 1) / BY, g.mz), tblock(32, BY, 1);
+#define CNS_RHS_CASE(SS, VV)                                                                       \
+    if (S == SS && V == VV) {                                                                      \
+        if constexpr (sizeof(R) == 4)                                                              \
+            k_rhs_tiled<R, SS, VV, BY><<<tgrid, tblock, 0, s>>>(g, cf, in, up, scal, quirk);       \
+        else                                                                                       \
+            k_rhs<R, SS, VV><<<grid, block, 0, s>>>(g, cf, in, up, scal, quirk);                   \
+        return;                                                                                    \
+    }
     CNS_RHS_CASE(1, 1)
     CNS_RHS_CASE(2, 1) CNS_RHS_CASE(2, 2)
     CNS_RHS_CASE(3, 1) CNS_RHS_CASE(3, 2) CNS_RHS_CASE(3, 3)

@@ -77,12 +77,28 @@ def test_driver_matches_library_and_restarts(tmp_path, gpu_lib):
     for a, b in zip(out2, s.copy_field_out()):
         np.testing.assert_array_equal(a, b)
     assert (tmp_path / "solution.txt").read_text().strip()
+    # XDMF descriptor: one uniform grid per written file, attributes pointing at them
+    import xml.etree.ElementTree as ET
+    root = ET.parse(tmp_path / "fields" / "fields.xmf").getroot()
+    grids = root.findall("./Domain/Grid/Grid")
+    assert [g.get("Name") for g in grids] == ["T0000000", "T0000001", "T0000002"]
+    for g in grids:
+        for att in g.findall("Attribute"):
+            fn = att.find("DataItem").text.strip()
+            assert (tmp_path / "fields" / fn).is_file()
+            assert att.find("DataItem").get("Dimensions").split() == ["24", "20", "16"]
+    times = [float(v) for v in root.find("./Domain/Grid/Time/DataItem").text.split()]
+    assert times[0] == 0.0 and times[1] < times[2]
     # restart from file 1 for one file reproduces file 2
     out_dir = tmp_path / "restart"
     (out_dir / "fields").mkdir(parents=True)
     for c in "ruvwe":
         os.link(tmp_path / "fields" / f"{c}.0000001.bin", out_dir / "fields" / f"{c}.0000001.bin")
+    os.link(tmp_path / "fields" / "scalars.0000001.txt", out_dir / "fields" / "scalars.0000001.txt")
     r = _run(out_dir, nsteps=4, nfiles=1, restart=1)
     assert r.returncode == 0, r.stderr
     for a, b in zip(read_fields(str(out_dir / "fields"), 2, p.shape), out2):
         np.testing.assert_array_equal(a, b)
+    # the restart continues the clock from the saved scalars
+    t_full = (tmp_path / "fields" / "scalars.0000002.txt").read_text()
+    assert (out_dir / "fields" / "scalars.0000002.txt").read_text() == t_full
