@@ -151,8 +151,10 @@ __global__ void __launch_bounds__(256, sizeof(R) == 4 ? 2 : 1) k_batch_stage(con
     }
     grid_barrier(bar, nb, err);
     // phase 5: RHS + stage update into the other state buffer. The unit's x-y neighbourhood
-    // of the nine stencil fields is staged in shared memory (as in the tiled single-solver
-    // kernel); z neighbours come from global memory.
+    // of the nine stencil fields is staged in shared memory, (32 + 2S) x (rows + 2S) per
+    // field, filled with coalesced row loads; z neighbours come from global memory. (Tile
+    // cells beyond the ghost layer, possible in the last unit of a row or column, are not
+    // read from memory; no thread uses them.)
     constexpr int TX = 32 + 2 * S, FSMAX = TX * (8 + 2 * S);
     __shared__ R tile[TF_COUNT * FSMAX];
     const int FS = TX * (rows + 2 * S), nt = blockDim.x;

@@ -20,17 +20,13 @@
 #include "cns_common.cuh"
 #include "cns_internal.h"
 
-#ifndef CNS_RHS_TILE_ROWS
-#define CNS_RHS_TILE_ROWS 4   // rows of a tiled RHS block (32 x rows threads)
-#endif
-
 namespace cns {
 
 template <typename R>
 __device__ __forceinline__ R ld(const R* __restrict__ p, long long o) { return __ldg(p + o); }
 
 // Neighbours of the centre point along one direction: in global memory at a stride, or in
-// the shared-memory plane tile of the tiled kernel (fields in the tile order TF_*).
+// a shared-memory plane tile (the persistent batch kernel; fields in the tile order TF_*).
 enum { TF_U, TF_V, TF_W, TF_R, TF_H, TF_P, TF_T, TF_M, TF_DIL, TF_COUNT };
 
 template <typename R>
@@ -335,39 +331,6 @@ __device__ __forceinline__ void rhs_point(const Geom& g, const CoefT<R>& cf, con
     rhs_point_nb<R, S, V>(g, cf, in, up, scal, quirk, i, k, c, nx, ny, nz, th0, m0, u0, v0, w0, r0, h0);
 }
 
-// The RHS kernel with the x-y neighbourhood of the nine stencil fields staged in shared
-// memory: per block one (32 + 2S) x (BY + 2S) tile per field, filled with coalesced row
-// loads; the x and y derivatives read the tile, the z derivatives global memory. Tile
-// cells beyond the ghost layer (possible in the last block of a row or column) are not
-// read from memory; no thread uses them.
-template <typename R, int S, int V, int BY>
-__global__ void __launch_bounds__(32 * BY, (sizeof(R) == 4 ? 768 : 512) / (32 * BY))
-    k_rhs_tiled(Geom g, CoefT<R> cf, RhsIn<R> in, Update<R> up, const double* __restrict__ scal, int quirk) {
-    constexpr int TX = 32 + 2 * S, TY = BY + 2 * S, FS = TX * TY, NT = 32 * BY;
-    __shared__ R tile[TF_COUNT * FS];
-    const int tx = threadIdx.x, ty = threadIdx.y, tid = ty * 32 + tx;
-    const int i0 = blockIdx.x * 32, j0 = blockIdx.y * BY, k = blockIdx.z;
-    const long long org = g.at(i0 - S, j0 - S, k);
-    const int xlim = g.mx + 2 * S - i0, ylim = g.my + 2 * S - j0;
-    const R* src[TF_COUNT] = {in.u, in.v, in.w, in.r, in.h, in.p, in.t, in.m, in.dil};
-#pragma unroll
-    for (int f = 0; f < TF_COUNT; f++) {
-        for (int e = tid; e < FS; e += NT) {
-            const int yy = e / TX, xx = e - yy * TX;
-            tile[f * FS + e] = (xx < xlim && yy < ylim) ? ld(src[f], org + (long long)yy * g.P + xx) : (R)0;
-        }
-    }
-    __syncthreads();
-    const int i = i0 + tx, j = j0 + ty;
-    if (i >= g.mx || j >= g.my) return;
-    const R* ctr = tile + (ty + S) * TX + (tx + S);
-    const NbTile<R> nx{ctr, 1, FS}, ny{ctr, TX, FS};
-    const long long c = g.at(i, j, k);
-    const NbGlobal<R> nz{&in, c, g.PS};
-    rhs_point_nb<R, S, V>(g, cf, in, up, scal, quirk, i, k, c, nx, ny, nz, ctr[TF_DIL * FS], ctr[TF_M * FS],
-                          ctr[TF_U * FS], ctr[TF_V * FS], ctr[TF_W * FS], ctr[TF_R * FS], ctr[TF_H * FS]);
-}
-
 template <typename R, int S, int V>
 __global__ void __launch_bounds__(128, sizeof(R) == 4 ? 6 : 4) k_rhs(Geom g, CoefT<R> cf, RhsIn<R> in, Update<R> up,
                                              const double* __restrict__ scal, int quirk) {
@@ -380,19 +343,9 @@ __global__ void __launch_bounds__(128, sizeof(R) == 4 ? 6 : 4) k_rhs(Geom g, Coe
 template <typename R>
 void launch_rhs_t(int S, int V, const Geom& g, const CoefT<R>& cf, const RhsIn<R>& in, const Update<R>& up,
                   const double* scal, int quirk, cudaStream_t s) {
-    // FP32: the shared-memory tiled kernel (latency-bound on neighbour loads otherwise);
-    // FP64: the FP64 pipe bounds the kernel, neighbours come through L1
-    constexpr int BY = CNS_RHS_TILE_ROWS;
     dim3 grid((g.mx + 31) / 32, (g.my + 3) / 4, g.mz), block(32, 4, 1);
-    dim3 tgrid((g.mx + 31) / 32, (g.my + BY - 1) / BY, g.mz), tblock(32, BY, 1);
-#define CNS_RHS_CASE(SS, VV)                                                                       \
-    if (S == SS && V == VV) {                                                                      \
-        if constexpr (sizeof(R) == 4)                                                              \
-            k_rhs_tiled<R, SS, VV, BY><<<tgrid, tblock, 0, s>>>(g, cf, in, up, scal, quirk);       \
-        else                                                                                       \
-            k_rhs<R, SS, VV><<<grid, block, 0, s>>>(g, cf, in, up, scal, quirk);                   \
-        return;                                                                                    \
-    }
+#define CNS_RHS_CASE(SS, VV) \
+    if (S == SS && V == VV) { k_rhs<R, SS, VV><<<grid, block, 0, s>>>(g, cf, in, up, scal, quirk); return; }
     CNS_RHS_CASE(1, 1)
     CNS_RHS_CASE(2, 1) CNS_RHS_CASE(2, 2)
     CNS_RHS_CASE(3, 1) CNS_RHS_CASE(3, 2) CNS_RHS_CASE(3, 3)
