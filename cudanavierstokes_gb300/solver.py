@@ -119,6 +119,18 @@ class Solver:
         native.check(native.lib().cns_calc_rhs(self._h, *[_ptr(f) for f in out]))
         return out
 
+    def plane_stats(self) -> np.ndarray:
+        """(11, mx): the columns of the reference's prof.txt (calcAvgChan), on the device."""
+        out = np.zeros((11, self.p.mx))
+        native.check(native.lib().cns_plane_stats(self._h, _ptr(out)))
+        return out
+
+    def friction_reynolds(self) -> float:
+        """The reference's printRes friction Reynolds number at the x = 0 wall, on the device."""
+        r = np.zeros(1)
+        native.check(native.lib().cns_friction_reynolds(self._h, _ptr(r)))
+        return float(r[0])
+
     def scalars(self) -> dict:
         a, b, c = (ctypes.c_double() for _ in range(3))
         native.check(native.lib().cns_get_scalars(self._h, ctypes.byref(a), ctypes.byref(b), ctypes.byref(c)))

@@ -202,6 +202,18 @@ CNS_API int64_t cns_kernel_launches(const cns_solver* h);
 /* Device bytes held by the handle. */
 CNS_API int64_t cns_device_bytes(const cns_solver* h);
 
+/* Plane profiles over (y, z) of the current state, the reference's calcAvgChan
+ * (src/init.cpp:150-208, its prof.txt) evaluated on the device: out[q * mx + i] for
+ * q = 0..10 = x, <rho>, <rho u>/<rho>, <rho v>/<rho>, <rho w>/<rho>, <rhoE>, and the
+ * (y, z) means of (rho - <rho>)^2, (u - ~u)^2, (v - ~v)^2, (w - ~w)^2, (rhoE - <rhoE>)^2. */
+CNS_API int cns_plane_stats(cns_solver* h, double* out);
+
+/* Friction Reynolds number at the x = 0 wall of the current state, the reference's
+ * printRes (src/init.cpp:210-256) on the device: the (y, z) mean of u_tau rho_w / mu_w,
+ * u_tau = sqrt(mu_w |dw/dx| / rho_w), mu_w = 1^viscexp / Re, dw/dx at the first point at
+ * the advective order from the interior values mirrored evenly about the wall. */
+CNS_API int cns_friction_reynolds(cns_solver* h, double* ret);
+
 /* Stateless device reductions of a caller-owned state, the reference's calcTimeStep
  * (deviceCalcDt + hostReduceToMin, src/calc_stress.cu:122-160, src/cuda_math.cu:308-333)
  * and the volume integrals of calcPressureGrad / calcBulk (src/calc_stress.cu:98-201,

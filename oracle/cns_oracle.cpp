@@ -778,6 +778,64 @@ double spline_eval(const double* xa, const double* ya, const double* y2, int n, 
 
 thread_local char g_err[256] = "";
 
+/* ---------------- src/init.cpp:150-208 calcAvgChan: plane profiles over (y, z) ----------------
+ * out[q * mx + i], q = 0..10: x, <rho>, <rho u>/<rho>, <rho v>/<rho>, <rho w>/<rho>, <rhoE>,
+ * then the plane means of (rho - <rho>)^2, (u - ~u)^2, (v - ~v)^2, (w - ~w)^2, (rhoE - <rhoE>)^2
+ * (the columns of the reference's prof.txt), each term divided by my*mz before summation. */
+void plane_stats(const Oracle& o, double* out) {
+    const int mx = o.mx, my = o.my, mz = o.mz;
+    for (int i = 0; i < mx; i++) {
+        double rm = 0, um = 0, vm = 0, wm = 0, em = 0;
+        for (int k = 0; k < mz; k++)
+            for (int j = 0; j < my; j++) {
+                const size_t c = o.id(i, j, k);
+                rm += o.r[c] / my / mz;
+                um += o.r[c] * o.u[c] / my / mz;
+                vm += o.r[c] * o.v[c] / my / mz;
+                wm += o.r[c] * o.w[c] / my / mz;
+                em += o.e[c] / my / mz;
+            }
+        um /= rm; vm /= rm; wm /= rm;
+        double rf = 0, uf = 0, vf = 0, wf = 0, ef = 0;
+        for (int k = 0; k < mz; k++)
+            for (int j = 0; j < my; j++) {
+                const size_t c = o.id(i, j, k);
+                rf += (o.r[c] - rm) * (o.r[c] - rm) / my / mz;
+                uf += (o.u[c] - um) * (o.u[c] - um) / my / mz;
+                vf += (o.v[c] - vm) * (o.v[c] - vm) / my / mz;
+                wf += (o.w[c] - wm) * (o.w[c] - wm) / my / mz;
+                ef += (o.e[c] - em) * (o.e[c] - em) / my / mz;
+            }
+        const double col[11] = {o.x[i], rm, um, vm, wm, em, rf, uf, vf, wf, ef};
+        for (int q = 0; q < 11; q++) out[(size_t)q * mx + i] = col[q];
+    }
+}
+
+/* ---------------- src/init.cpp:210-256 printRes: friction Reynolds number at x = 0 ----------------
+ * Re_tau = < u_tau rho_w / mu_w > over (y, z), u_tau = sqrt(mu_w |dw/dx| / rho_w), mu_w = 1/Re
+ * (T_w = 1), dw/dx at the first point from the interior values mirrored evenly about the
+ * wall, at the advective order, times x'(0)^-1 (xp[0]). */
+double friction_reynolds(const Oracle& o) {
+    const int S = o.S;
+    double Ret = 0.0;
+    for (int k = 0; k < o.mz; k++)
+        for (int j = 0; j < o.my; j++) {
+            const double temw = 1.0;
+            const double suth = pow(temw, o.p.viscexp);
+            const double muw = suth / o.p.Re;
+            double ub[9];
+            for (int i = S; i < S * 2 + 1; i++) ub[i] = o.w[o.id(i - S, j, k)];
+            for (int i = 0; i < S; i++) ub[i] = o.w[o.id(S - i - 1, j, k)];
+            double dudx = 0;
+            for (int i = 0; i < S; i++) dudx += o.cF[i] * (ub[i] - ub[S * 2 - i]) / o.dxr;
+            dudx *= o.xp[0];
+            const double rw = o.r[o.id(0, j, k)];
+            const double ut = sqrt(muw * fabs(dudx) / rw);
+            Ret += ut * rw / muw;
+        }
+    return Ret / o.my / o.mz;
+}
+
 }  // namespace
 
 extern "C" {
@@ -986,6 +1044,16 @@ int cnso_get_scalars(void* h, double* dt, double* dpdz, double* time) {
 int cnso_set_scalars(void* h, double dt, double dpdz, double time) {
     Oracle* o = (Oracle*)h;
     o->dt = dt; o->dpdz = dpdz; o->time = time;
+    return 0;
+}
+
+int cnso_plane_stats(void* h, double* out) {
+    plane_stats(*(Oracle*)h, out);
+    return 0;
+}
+
+int cnso_friction_reynolds(void* h, double* ret) {
+    *ret = friction_reynolds(*(Oracle*)h);
     return 0;
 }
 

@@ -71,6 +71,8 @@ def lib():
         L.cnso_run.argtypes = [v, ctypes.c_int] + [_dp] * 5
         L.cnso_get_scalars.argtypes = [v, _dp, _dp, _dp]
         L.cnso_set_scalars.argtypes = [v, ctypes.c_double, ctypes.c_double, ctypes.c_double]
+        L.cnso_plane_stats.argtypes = [v, _dp]
+        L.cnso_friction_reynolds.argtypes = [v, _dp]
         _lib = L
     return _lib
 
@@ -163,6 +165,18 @@ class Oracle:
         d = np.zeros(1)
         lib().cnso_calc_dt(self.h, _ptr(d))
         return float(d[0])
+
+    def plane_stats(self):
+        """calcAvgChan (src/init.cpp:150-208): (11, mx) = the columns of prof.txt."""
+        out = np.zeros((11, self.p.mx))
+        lib().cnso_plane_stats(self.h, _ptr(out))
+        return out
+
+    def friction_reynolds(self):
+        """printRes (src/init.cpp:210-256): the average friction Reynolds number."""
+        r = np.zeros(1)
+        lib().cnso_friction_reynolds(self.h, _ptr(r))
+        return float(r[0])
 
     def bulk(self):
         a, b = np.zeros(1), np.zeros(1)

@@ -14,7 +14,9 @@ reference itself. Steps:
           profiles blasius1D/*.bin) and a Makefile.
   run     (on the GPU machine) `make` each case for sm_103a and run ./ns with
           CUDA_LAUNCH_BLOCKING=1 (program order: the reference's streams race otherwise),
-          then pack initial and final fields and the dt/dpdz log into
+          then pack initial and final fields, the dt/dpdz log, the friction Reynolds
+          number the reference prints for the initial field (printRes) and its prof.txt
+          plane profiles of the final field (calcAvgChan) into
           gpurun_out/ref_golden/<case>.npz.
   collect (back in the container) copy the packed results to tests/golden/.
 
@@ -271,11 +273,15 @@ def run(names):
         out = initial.read_fields(os.path.join(d, "fields"), 1, shape)
         steps = [(int(m.group(1)), float(m.group(2)), float(m.group(3)))
                  for m in re.finditer(r"step number (\d+) with (\S+) (\S+)", log)]
+        m = re.search(r"friction Reynolds number is:\s+(\S+)", log)
+        ret = np.array([float(m.group(1)) if m else np.nan])
+        prof_path = os.path.join(d, "prof.txt")
+        prof = np.loadtxt(prof_path) if os.path.exists(prof_path) else np.zeros((0, 11))
         np.savez_compressed(os.path.join(OUT_ROOT, name + ".npz"),
                             ic=np.stack(ic), out=np.stack(out),
                             x=np.fromfile(os.path.join(d, "fields", "x.bin")),
                             steplog=np.array(steps, dtype=np.float64).reshape(-1, 3),
-                            meta=json.dumps(meta))
+                            ret=ret, prof=prof, meta=json.dumps(meta))
         print(f"[{name}] ok: {len(steps)} dt lines, rho range {out[0].min():.6f}..{out[0].max():.6f}")
     return ok
 

@@ -25,7 +25,8 @@ def load(name):
     for k, v in meta["params"].items():
         setattr(p, k, v)
     return dict(params=p, nsteps=int(meta["nsteps"]), ic=[a.copy() for a in z["ic"]],
-                out=[a.copy() for a in z["out"]], x=z["x"].copy(), steplog=z["steplog"].copy(), kind=meta["ic"])
+                out=[a.copy() for a in z["out"]], x=z["x"].copy(), steplog=z["steplog"].copy(), kind=meta["ic"],
+                ret=float(z["ret"][0]) if "ret" in z else None, prof=z["prof"].copy() if "prof" in z else None)
 
 
 def sponge_from_ic(case, strengths):

@@ -29,3 +29,17 @@ def test_oracle_matches_reference(oracle_mod, name):
     # the reference prints dt with 7 significant digits at every dt update
     for step, dt, _ in c["steplog"]:
         assert abs(logs["dt"][int(step)] - dt) <= 5e-7 * dt
+
+
+@pytest.mark.parametrize("name", golden_cases.names())
+def test_oracle_statistics_match_reference(oracle_mod, name):
+    """calcAvgChan's prof.txt (final fields) and printRes's friction Reynolds number
+    (initial fields) as printed by the reference (%lf: 6 decimals)."""
+    case = golden_cases.load(name)
+    o = oracle_mod.Oracle(case["params"])
+    o.set_state(*case["ic"])
+    assert abs(o.friction_reynolds() - case["ret"]) <= 5.01e-7
+    o.set_state(*case["out"])
+    prof = o.plane_stats().T
+    assert prof.shape == case["prof"].shape
+    assert np.abs(prof - case["prof"]).max() <= 5.01e-7
