@@ -9,7 +9,8 @@
 // checkCFLcondition, checkBulk, Re, Pr, Ma, viscexp, gam, stretch, TwallTop, TwallBot) plus
 // optional precision (0 FP64, 1 FP32 RHS) and quirk_dissipation_y. Output as the reference:
 // fields/{x,y,z}.bin, Grid.txt, fields/{r,u,v,w,e}.%07d.bin (raw FP64, [k][j][i]),
-// solution.txt ("step time kin par2 dtime" every checkCFLcondition steps), and an XDMF
+// solution.txt ("step time kin par2 dtime" every checkCFLcondition steps), prof.txt (plane
+// profiles, after each file) and the printed friction Reynolds number, and an XDMF
 // descriptor fields/fields.xmf of the files this run wrote. A boundary layer
 // reads blasius1D/{x,r,u,w,e}Prof.bin. Without restart the initial field is the reference's
 // own: initChannel (forcing), initCHIT (periodic box) or the sponge reference fields.
@@ -122,6 +123,19 @@ void write_scalars(cns_solver* h, const std::string& dir, int step) {
     cns_get_scalars(h, &dt, &dpdz, &t);
     if (FILE* f = fopen(scalars_name(dir, step).c_str(), "w")) {
         fprintf(f, "time = %.17g\ndt = %.17g\ndpdz = %.17g\n", t, dt, dpdz);
+        fclose(f);
+    }
+}
+
+// calcAvgChan's prof.txt (src/init.cpp:150-208) from the device plane statistics
+void write_prof(cns_solver* h, const std::string& dir, int mx) {
+    std::vector<double> st(11 * (size_t)mx);
+    if (cns_plane_stats(h, st.data()) != CNS_OK) return;
+    if (FILE* f = fopen((dir + "/prof.txt").c_str(), "w")) {
+        for (int i = 0; i < mx; i++) {
+            for (int q = 0; q < 11; q++) fprintf(f, q ? "\t%lf" : "%lf", st[(size_t)q * mx + i]);
+            fprintf(f, "\n");
+        }
         fclose(f);
     }
 }
@@ -273,6 +287,10 @@ int main(int argc, char** argv) {
             cns_set_scalars(h, std::strtod(sc["dt"].c_str(), nullptr), std::strtod(sc["dpdz"].c_str(), nullptr),
                             std::strtod(sc["time"].c_str(), nullptr), -1);
     }
+    // printRes and calcAvgChan of the initial field (src/main.cpp:58-59)
+    double ret = 0;
+    if (cns_friction_reynolds(h, &ret) == CNS_OK) printf("\nThe average friction Reynolds number is: \t %lf\n", ret);
+    write_prof(h, dir, p.mx);
     std::vector<std::pair<int, double>> written;
     {
         double t0 = 0;
@@ -303,6 +321,7 @@ int main(int argc, char** argv) {
         for (int q = 0; q < 5; q++) write_bin(field_name(dir, names[q], file), f[q].data(), N);
         write_scalars(h, dir, file);
         written.push_back({file, tim[nsteps - 1]});
+        write_prof(h, dir, p.mx);   // calcAvgChan after each file (src/cuda_main.cu:311)
         printf("file number: %d  \t step: %d  \t time: %lf  \t kin: %le  \t energy: %le\n", file, file * nsteps,
                tim[nsteps - 1], par1[0], par2[0]);
         if (sol)

@@ -77,6 +77,10 @@ def test_driver_matches_library_and_restarts(tmp_path, gpu_lib):
     for a, b in zip(out2, s.copy_field_out()):
         np.testing.assert_array_equal(a, b)
     assert (tmp_path / "solution.txt").read_text().strip()
+    # prof.txt: the plane profiles of the last file, as the reference writes them
+    prof = np.loadtxt(tmp_path / "prof.txt")
+    np.testing.assert_allclose(prof, s.plane_stats().T, rtol=0, atol=5.01e-7)
+    assert "friction Reynolds number" in r.stdout
     # XDMF descriptor: one uniform grid per written file, attributes pointing at them
     import xml.etree.ElementTree as ET
     root = ET.parse(tmp_path / "fields" / "fields.xmf").getroot()

@@ -115,6 +115,29 @@ def test_sponge_profile_interpolation(gpu_lib, oracle_mod):
     assert np.all(v == 0)
 
 
+def test_boundary_layer_from_generated_inflow(gpu_lib, oracle_mod):
+    """The self-similar inflow profiles of cudanavierstokes_gb300.blasius through the sponge
+    spline into the reference fields, then three steps, against the oracle."""
+    pytest.importorskip("scipy")
+    from cudanavierstokes_gb300.blasius import self_similar_profiles
+    p = boundary_layer_params(16, 8, 160)
+    prof = self_similar_profiles(p.gam, p.Ma, p.Pr)
+    args = [prof[k] for k in ("x", "r", "u", "w", "e")]
+    o = oracle_mod.Oracle(p)
+    spx, spz = o.sponge_strengths()
+    rref, uref, wref, eref = o.sponge_refs(*args)
+    o.set_sponge(spx, spz, rref, uref, wref, eref)
+    o.set_state(*[np.broadcast_to(a[:, None, :], p.shape).copy()
+                  for a in (rref, uref, np.zeros_like(rref), wref, eref)])
+    s = Solver(p)
+    s.set_sponge_profiles(*args, init_fields=True)
+    for a, b in zip(s.copy_field_out(), o.get_state()):
+        assert rel_err(a, b) <= 1e-14
+    o.run(3)
+    s.run(3)
+    assert max(state_errors(s.copy_field_out(), o.get_state())) <= TOL64
+
+
 @pytest.mark.parametrize("case", ["tgv_s4v4", "tgv_classic_s2v1", "channel_s3v2", "channel_s4v4", "bl_s3v2",
                                   "tgv_rk4"])
 def test_run_parity(gpu_lib, oracle_mod, case):
