@@ -182,7 +182,7 @@ __global__ void __launch_bounds__(256, sizeof(R) == 4 ? 2 : 1) k_batch_stage(con
             for (int f = 0; f < TF_COUNT; f++) {
                 for (int e = threadIdx.x; e < FS; e += nt) {
                     const int yy = e / TX, xx = e - yy * TX;
-                    tile[f * FS + e] = (xx < xlim && yy < ylim) ? ld(src[f], org + (long long)yy * P + xx) : (R)0;
+                    tile[f * FS + e] = (xx < xlim && yy < ylim) ? ld(src[f], (int)(org + (long long)yy * P + xx)) : (R)0;
                 }
             }
         }
@@ -199,8 +199,8 @@ __global__ void __launch_bounds__(256, sizeof(R) == 4 ? 2 : 1) k_batch_stage(con
             up.wref = I.wref; up.eref = I.eref;
             const R* ctr = tile + (ty + S) * TX + (tx + S);
             const NbTile<R> nbx{ctr, 1, FS}, nby{ctr, TX, FS};
-            const long long c = I.g.at(i, j, k);
-            const NbGlobal<R> nbz{&in, c, I.g.PS};
+            const int c = (int)I.g.at(i, j, k);
+            const NbGlobal<R> nbz{&in, c, (int)I.g.PS};
             rhs_point_nb<R, S, V>(I.g, I.cf, in, up, I.scal, quirk, i, k, c, nbx, nby, nbz, ctr[TF_DIL * FS],
                                   ctr[TF_M * FS], ctr[TF_U * FS], ctr[TF_V * FS], ctr[TF_W * FS], ctr[TF_R * FS],
                                   ctr[TF_H * FS]);

@@ -23,16 +23,19 @@
 namespace cns {
 
 template <typename R>
-__device__ __forceinline__ R ld(const R* __restrict__ p, long long o) { return __ldg(p + o); }
+__device__ __forceinline__ R ld(const R* __restrict__ p, int o) { return __ldg(p + o); }
 
 // Neighbours of the centre point along one direction: in global memory at a stride, or in
 // a shared-memory plane tile (the persistent batch kernel; fields in the tile order TF_*).
 enum { TF_U, TF_V, TF_W, TF_R, TF_H, TF_P, TF_T, TF_M, TF_DIL, TF_COUNT };
 
+// Element offsets are 32-bit: every padded field holds fewer than 2^31 elements (checked
+// when a solver is created), and 64-bit offset arithmetic costs two integer instructions
+// per neighbour address.
 template <typename R>
 struct NbGlobal {
     const RhsIn<R>* in;
-    long long c, st;
+    int c, st;
     __device__ __forceinline__ R u(int l) const { return ld(in->u, c + l * st); }
     __device__ __forceinline__ R v(int l) const { return ld(in->v, c + l * st); }
     __device__ __forceinline__ R w(int l) const { return ld(in->w, c + l * st); }
@@ -217,7 +220,7 @@ __device__ __forceinline__ void rhs_direction(const Geom& g, const CoefT<R>& cf,
 template <typename R, int S, int V, class NX, class NY, class NZ>
 __device__ __forceinline__ void rhs_point_nb(const Geom& g, const CoefT<R>& cf, const RhsIn<R>& in,
                                              const Update<R>& up, const double* __restrict__ scal, int quirk, int i,
-                                             int k, long long c, const NX& nx, const NY& ny, const NZ& nz, R th0,
+                                             int k, int c, const NX& nx, const NY& ny, const NZ& nz, R th0,
                                              R m0, R u0, R v0, R w0, R r0, R h0) {
     R Gr[9];
 #pragma unroll
@@ -324,10 +327,10 @@ __device__ __forceinline__ void rhs_point_nb(const Geom& g, const CoefT<R>& cf, 
 template <typename R, int S, int V>
 __device__ __forceinline__ void rhs_point(const Geom& g, const CoefT<R>& cf, const RhsIn<R>& in, const Update<R>& up,
                                           const double* __restrict__ scal, int quirk, int i, int j, int k) {
-    const long long c = g.at(i, j, k);
+    const int c = (int)g.at(i, j, k);
     const R th0 = ld(in.dil, c), m0 = ld(in.m, c);
     const R u0 = ld(in.u, c), v0 = ld(in.v, c), w0 = ld(in.w, c), r0 = ld(in.r, c), h0 = ld(in.h, c);
-    const NbGlobal<R> nx{&in, c, 1LL}, ny{&in, c, g.P}, nz{&in, c, g.PS};
+    const NbGlobal<R> nx{&in, c, 1}, ny{&in, c, (int)g.P}, nz{&in, c, (int)g.PS};
     rhs_point_nb<R, S, V>(g, cf, in, up, scal, quirk, i, k, c, nx, ny, nz, th0, m0, u0, v0, w0, r0, h0);
 }
 

@@ -79,6 +79,13 @@ int check_params(const cns_params* p) {
         return fail(CNS_ERR_INVALID, "grid %dx%dx%d too small for stencil half-width %d", p->mx, p->my, p->mz, S);
     if ((long long)p->mx * p->my * p->mz > (1LL << 34))
         return fail(CNS_ERR_INVALID, "grid too large");
+    {
+        // the stencil kernels address a padded field with 32-bit element offsets
+        const long long G = S, P = ((16 + p->mx + G) + 15) / 16 * 16;
+        if (P * (p->my + 2 * G) * (p->mz + 2 * G) >= (1LL << 31))
+            return fail(CNS_ERR_INVALID, "grid %dx%dx%d too large: a padded field must hold fewer than 2^31 elements",
+                        p->mx, p->my, p->mz);
+    }
     if (!(p->Lx > 0) || !(p->Ly > 0) || !(p->Lz > 0)) return fail(CNS_ERR_INVALID, "domain lengths must be > 0");
     if (!(p->Re > 0) || !(p->Pr > 0) || !(p->Ma > 0) || !(p->gam > 1) || !(p->cfl > 0))
         return fail(CNS_ERR_INVALID, "Re, Pr, Ma, cfl must be > 0 and gam > 1");
