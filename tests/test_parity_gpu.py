@@ -201,6 +201,23 @@ def test_fp32_rhs_channel(gpu_lib, oracle_mod):
     assert max(errs) <= 1e-4, errs
 
 
+def test_fp32_rhs_plane_marching_kernel(gpu_lib, oracle_mod):
+    """A grid large enough for the FP32 RHS kernel that streams z planes through shared
+    memory by TMA (stretched channel with walls), against the FP64 oracle: one RHS and
+    five steps."""
+    p = channel_params(64, 64, 48)
+    o = oracle_mod.Oracle(p)
+    f = wall_state(p, o.grid()["x"])
+    o.set_state(*f)
+    s = Solver(p.copy(precision=PREC_FP32_RHS))
+    s.copy_field_in(*f)
+    errs = field_errors(s.calc_rhs(), o.rhs())
+    assert max(errs) <= 1e-4, errs
+    o.run(5)
+    s.run(5)
+    assert max(state_errors(s.copy_field_out(), o.get_state())) <= 2e-6
+
+
 def test_rk4_third_order_or_better(gpu_lib):
     """RK4 (no counterpart in the reference): halving dt cuts the error against a fine
     reference run by at least 2^3."""
