@@ -155,9 +155,10 @@ BatchInst<R> make_inst(cns_solver* h, int rows, int64_t cap) {
     I.tlog = h->tlog;
     for (int c = 0; c < 2; c++)
         for (int f = 0; f < 5; f++) I.q[c][f] = h->q[c][f];
-    for (int f = 0; f < 4; f++) I.der[f] = (R*)h->der[f];
+    // the persistent kernel recovers each stage's state itself, into the derived buffer 0
+    for (int f = 0; f < 4; f++) I.der[f] = (R*)h->der[0][f];
     for (int f = 0; f < 5; f++) I.rb[f] = (R*)h->rb[f];
-    for (int f = 0; f < 4; f++) I.s32[f] = h->fp32 ? (R*)h->s32[f] : nullptr;
+    for (int f = 0; f < 4; f++) I.s32[f] = h->fp32 ? (R*)h->s32[0][f] : nullptr;
     I.dil = (R*)h->dil;
     for (int f = 0; f < 9; f++) I.grad[f] = (R*)h->grad[f];
     if (h->has_sponge) {
@@ -482,7 +483,15 @@ int cns_batch_step(cns_batch* b, int nsteps) {
             if (want && (rc = cns::solver_reduce(h, want, dg))) return rc;
         }
         if ((rc = b->mode == CNS_BATCH_CONCURRENT ? step_members(b) : step_stages(b))) return rc;
-        for (auto& m : b->members) m.steps++;
+        for (auto& m : b->members) {
+            m.steps++;
+            if (b->mode != CNS_BATCH_CONCURRENT) {
+                // derived buffer 0 holds the recovery of the last stage's input state: the
+                // latest one in the reference's order, not that of the current state
+                m.h->der_ok[0] = m.h->der_ok[1] = false;
+                m.h->mu_buf = 0;
+            }
+        }
     }
     BCK(cudaStreamSynchronize(b->stream));
     int err = 0;

@@ -191,6 +191,7 @@ __global__ void __launch_bounds__(256, sizeof(R) == 4 ? 2 : 1) k_batch_stage(con
         if (i < I.g.mx && j < I.g.my) {
             Update<R> up;
             up.kind = kind; up.a = a; up.b = b; up.ca = (R)a; up.cb = (R)b; up.use_prev = a != 0.0;
+            up.fuse = 0;   // this kernel recovers each stage's state in its own phase
             up.qin = StateIn{I.q[cur][0], I.q[cur][1], I.q[cur][2], I.q[cur][3], I.q[cur][4]};
             const int nx = 1 - cur;
             up.qout = StateOut{I.q[nx][0], I.q[nx][1], I.q[nx][2], I.q[nx][3], I.q[nx][4]};

@@ -70,11 +70,16 @@ struct Update {
     double* q0[5];          // classic schemes: conserved state at the step start
     // sponge (boundary layer): strengths and reference fields on the (x,z) plane
     const double *spx, *spz, *rref, *uref, *vref, *wref, *eref;
+    // fused state recovery of the new state (calcState of the next stage): 0 = off
+    int fuse;
+    DerivedOut<R> dnext;
+    Phys ph;
 };
 
 template <typename R>
 void launch_state(const Geom& g, const Phys& ph, const StateIn& q, const DerivedOut<R>& o, double* scal,
                   int advance_time, double* time_log, long long tcap, cudaStream_t s);
+void launch_advance_time(double* scal, double* time_log, long long tcap, cudaStream_t s);
 template <typename R>
 void launch_ghost_state(const Geom& g, const Phys& ph, const StencilFields<R>& f, const double* scal, cudaStream_t s);
 template <typename R>
@@ -94,8 +99,8 @@ void launch_pack(const Geom& g, const T* src, double* dst, cudaStream_t s);
 int set_error(int code, const char* msg);
 
 void launch_rhs_fp64(int S, int V, const Geom& g, const Phys& ph, const CoefT<double>& cf, const RhsIn<double>& in,
-                     const Update<double>& up, const double* scal, int quirk, cudaStream_t s);
+                     const Update<double>& up, double* scal, int quirk, cudaStream_t s);
 void launch_rhs_fp32(int S, int V, const Geom& g, const Phys& ph, const CoefT<float>& cf, const RhsIn<float>& in,
-                     const Update<float>& up, const double* scal, int quirk, cudaStream_t s);
+                     const Update<float>& up, double* scal, int quirk, cudaStream_t s);
 
 }  // namespace cns

@@ -13,12 +13,11 @@ namespace cns {
 // mode the FP32 stencil copies of rho, u, v, w are written too and mu is evaluated in
 // FP32 from the FP64 T.
 // ---------------------------------------------------------------------------------
+// T, p, H, mu (and the FP32 copies) of one point from its FP64 state and 1/rho; the state
+// kernel and the fused epilogue of the RHS kernel share it
 template <typename R>
-__device__ __forceinline__ void state_point(const Geom& g, const Phys& ph, const StateIn& q, const DerivedOut<R>& o,
-                                            double* scal, int i, int j, int k) {
-    const long long c = g.at(i, j, k);
-    const double rr = q.r[c], uu = q.u[c], vv = q.v[c], ww = q.w[c], ee = q.e[c];
-    const double inv = rcp_nr(rr);
+__device__ __forceinline__ void state_store(const Phys& ph, const DerivedOut<R>& o, double* scal, long long c,
+                                            double rr, double inv, double uu, double vv, double ww, double ee) {
     const double en = ee * inv - 0.5 * (uu * uu + vv * vv + ww * ww);
     const double T = ph.cvInv * en;
     const double pr = rr * ph.Rgas * T;
@@ -42,6 +41,14 @@ __device__ __forceinline__ void state_point(const Geom& g, const Phys& ph, const
         o.m[c] = (R)(suth * ph.invRe);
         if (!(T > 0.0) || !(rr > 0.0)) scal[SC_NONFINITE] = 1.0;   // racy flag write, any writer is fine
     }
+}
+
+template <typename R>
+__device__ __forceinline__ void state_point(const Geom& g, const Phys& ph, const StateIn& q, const DerivedOut<R>& o,
+                                            double* scal, int i, int j, int k) {
+    const long long c = g.at(i, j, k);
+    const double rr = q.r[c], uu = q.u[c], vv = q.v[c], ww = q.w[c], ee = q.e[c];
+    state_store<R>(ph, o, scal, c, rr, rcp_nr(rr), uu, vv, ww, ee);
 }
 
 // Stage 0 of a step advances the simulation time by dt (deviceAdvanceTime) and, with a

@@ -19,6 +19,7 @@
 #pragma once
 #include "cns_common.cuh"
 #include "cns_internal.h"
+#include "kernels_point.cuh"
 
 namespace cns {
 
@@ -219,7 +220,7 @@ __device__ __forceinline__ void rhs_direction(const Geom& g, const CoefT<R>& cf,
 // along x, y, z from the accessors nx, ny, nz and the centre values given
 template <typename R, int S, int V, class NX, class NY, class NZ>
 __device__ __forceinline__ void rhs_point_nb(const Geom& g, const CoefT<R>& cf, const RhsIn<R>& in,
-                                             const Update<R>& up, const double* __restrict__ scal, int quirk, int i,
+                                             const Update<R>& up, double* __restrict__ scal, int quirk, int i,
                                              int k, int c, const NX& nx, const NY& ny, const NZ& nz, R th0,
                                              R m0, R u0, R v0, R w0, R r0, R h0) {
     R Gr[9];
@@ -316,17 +317,21 @@ __device__ __forceinline__ void rhs_point_nb(const Geom& g, const CoefT<R>& cf, 
         }
     }
     const double inv = rcp_nr(qn[0]);
+    const double un = qn[1] * inv, vn = qn[2] * inv, wn = qn[3] * inv;
     up.qout.r[c] = qn[0];
-    up.qout.u[c] = qn[1] * inv;
-    up.qout.v[c] = qn[2] * inv;
-    up.qout.w[c] = qn[3] * inv;
+    up.qout.u[c] = un;
+    up.qout.v[c] = vn;
+    up.qout.w[c] = wn;
     up.qout.e[c] = qn[4];
+    // the next stage's state recovery from the values in registers (bit for bit the state
+    // kernel's result on the stored state)
+    if (up.fuse) state_store<R>(up.ph, up.dnext, scal, c, qn[0], inv, un, vn, wn, qn[4]);
 }
 
 // RHS + stage update of one interior point (i, j, k), every neighbour from global memory
 template <typename R, int S, int V>
 __device__ __forceinline__ void rhs_point(const Geom& g, const CoefT<R>& cf, const RhsIn<R>& in, const Update<R>& up,
-                                          const double* __restrict__ scal, int quirk, int i, int j, int k) {
+                                          double* __restrict__ scal, int quirk, int i, int j, int k) {
     const int c = (int)g.at(i, j, k);
     const R th0 = ld(in.dil, c), m0 = ld(in.m, c);
     const R u0 = ld(in.u, c), v0 = ld(in.v, c), w0 = ld(in.w, c), r0 = ld(in.r, c), h0 = ld(in.h, c);
@@ -336,7 +341,7 @@ __device__ __forceinline__ void rhs_point(const Geom& g, const CoefT<R>& cf, con
 
 template <typename R, int S, int V>
 __global__ void __launch_bounds__(128, sizeof(R) == 4 ? 6 : 4) k_rhs(Geom g, CoefT<R> cf, RhsIn<R> in, Update<R> up,
-                                             const double* __restrict__ scal, int quirk) {
+                                             double* __restrict__ scal, int quirk) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     const int j = blockIdx.y * blockDim.y + threadIdx.y;
     if (i >= g.mx || j >= g.my) return;
@@ -345,7 +350,7 @@ __global__ void __launch_bounds__(128, sizeof(R) == 4 ? 6 : 4) k_rhs(Geom g, Coe
 
 template <typename R>
 void launch_rhs_t(int S, int V, const Geom& g, const CoefT<R>& cf, const RhsIn<R>& in, const Update<R>& up,
-                  const double* scal, int quirk, cudaStream_t s) {
+                  double* scal, int quirk, cudaStream_t s) {
     dim3 grid((g.mx + 31) / 32, (g.my + 3) / 4, g.mz), block(32, 4, 1);
 #define CNS_RHS_CASE(SS, VV) \
     if (S == SS && V == VV) { k_rhs<R, SS, VV><<<grid, block, 0, s>>>(g, cf, in, up, scal, quirk); return; }

@@ -3,7 +3,7 @@
 
 namespace cns {
 void launch_rhs_fp64(int S, int V, const Geom& g, const Phys&, const CoefT<double>& cf, const RhsIn<double>& in,
-                     const Update<double>& up, const double* scal, int quirk, cudaStream_t s) {
+                     const Update<double>& up, double* scal, int quirk, cudaStream_t s) {
     launch_rhs_t<double>(S, V, g, cf, in, up, scal, quirk, s);
 }
 }  // namespace cns

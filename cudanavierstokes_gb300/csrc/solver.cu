@@ -103,14 +103,15 @@ int check_params(const cns_params* p) {
 template <typename R>
 RhsIn<R> rhs_in(cns_solver* h) {
     RhsIn<R> in;
+    const int c = h->cur;
     if (h->fp32) {
-        in.r = (const R*)h->s32[0]; in.u = (const R*)h->s32[1]; in.v = (const R*)h->s32[2]; in.w = (const R*)h->s32[3];
+        in.r = (const R*)h->s32[c][0]; in.u = (const R*)h->s32[c][1]; in.v = (const R*)h->s32[c][2];
+        in.w = (const R*)h->s32[c][3];
     } else {
-        in.r = (const R*)h->q[h->cur][0]; in.u = (const R*)h->q[h->cur][1];
-        in.v = (const R*)h->q[h->cur][2]; in.w = (const R*)h->q[h->cur][3];
+        in.r = (const R*)h->q[c][0]; in.u = (const R*)h->q[c][1]; in.v = (const R*)h->q[c][2]; in.w = (const R*)h->q[c][3];
     }
-    in.h = (const R*)h->der[0]; in.t = (const R*)h->der[1]; in.p = (const R*)h->der[2];
-    in.m = (const R*)h->der[3]; in.dil = (const R*)h->dil;
+    in.h = (const R*)h->der[c][0]; in.t = (const R*)h->der[c][1]; in.p = (const R*)h->der[c][2];
+    in.m = (const R*)h->der[c][3]; in.dil = (const R*)h->dil;
     for (int q = 0; q < 9; q++) in.g[q] = (const R*)h->grad[q];
     return in;
 }
@@ -119,24 +120,44 @@ StateIn state_in(cns_solver* h, int b) {
     return StateIn{h->q[b][0], h->q[b][1], h->q[b][2], h->q[b][3], h->q[b][4]};
 }
 
-// calcState + ghost fill for the current state
+// derived-field outputs of state buffer b
 template <typename R>
-int state_phase(cns_solver* h, int advance_time, double* time_log) {
+DerivedOut<R> derived_out(cns_solver* h, int b) {
     DerivedOut<R> o;
-    o.h = (R*)h->der[0]; o.t = (R*)h->der[1]; o.p = (R*)h->der[2]; o.m = (R*)h->der[3];
+    o.h = (R*)h->der[b][0]; o.t = (R*)h->der[b][1]; o.p = (R*)h->der[b][2]; o.m = (R*)h->der[b][3];
     o.r32 = o.u32 = o.v32 = o.w32 = nullptr;
+    if (h->fp32) {
+        o.r32 = (R*)h->s32[b][0]; o.u32 = (R*)h->s32[b][1]; o.v32 = (R*)h->s32[b][2]; o.w32 = (R*)h->s32[b][3];
+    }
+    return o;
+}
+
+// calcState of the current state (when the RHS kernel has not recovered it already)
+template <typename R>
+int state_phase(cns_solver* h) {
+    launch_state<R>(h->geom, h->phys, state_in(h, h->cur), derived_out<R>(h, h->cur), h->scal, 0, nullptr, 0,
+                    h->stream);
+    h->launches += 1;
+    CKL();
+    h->der_ok[h->cur] = true;
+    h->mu_buf = h->cur;
+    return CNS_OK;
+}
+
+// ghost cells of the stencil inputs of the current state
+template <typename R>
+int ghost_phase(cns_solver* h) {
+    const int c = h->cur;
+    const DerivedOut<R> o = derived_out<R>(h, c);
     StencilFields<R> f;
     if (h->fp32) {
-        o.r32 = (R*)h->s32[0]; o.u32 = (R*)h->s32[1]; o.v32 = (R*)h->s32[2]; o.w32 = (R*)h->s32[3];
         f.r = o.r32; f.u = o.u32; f.v = o.v32; f.w = o.w32;
     } else {
-        f.r = (R*)h->q[h->cur][0]; f.u = (R*)h->q[h->cur][1]; f.v = (R*)h->q[h->cur][2]; f.w = (R*)h->q[h->cur][3];
+        f.r = (R*)h->q[c][0]; f.u = (R*)h->q[c][1]; f.v = (R*)h->q[c][2]; f.w = (R*)h->q[c][3];
     }
     f.t = o.t; f.p = o.p; f.h = o.h; f.m = o.m;
-    launch_state<R>(h->geom, h->phys, state_in(h, h->cur), o, h->scal, advance_time, time_log, h->diag_cap,
-                    h->stream);
     launch_ghost_state<R>(h->geom, h->phys, f, h->scal, h->stream);
-    h->launches += 2;
+    h->launches += 1;
     CKL();
     return CNS_OK;
 }
@@ -147,7 +168,7 @@ int grad_phase(cns_solver* h) {
     for (int q = 0; q < 9; q++) o.g[q] = (R*)h->grad[q];
     o.dil = (R*)h->dil;
     const R *u, *v, *w;
-    if (h->fp32) { u = (const R*)h->s32[1]; v = (const R*)h->s32[2]; w = (const R*)h->s32[3]; }
+    if (h->fp32) { u = (const R*)h->s32[h->cur][1]; v = (const R*)h->s32[h->cur][2]; w = (const R*)h->s32[h->cur][3]; }
     else { u = (const R*)h->q[h->cur][1]; v = (const R*)h->q[h->cur][2]; w = (const R*)h->q[h->cur][3]; }
     const CoefT<R>* cfp;
     if constexpr (std::is_same<R, float>::value) cfp = &h->cf32; else cfp = &h->cf64;
@@ -180,6 +201,11 @@ int rhs_phase(cns_solver* h, int kind, double a, double b) {
         up.spx = h->spx; up.spz = h->spz; up.rref = h->rref; up.uref = h->uref; up.vref = h->vref;
         up.wref = h->wref; up.eref = h->eref;
     }
+    if (kind != ST_RHS_ONLY) {   // the new state's recovery for the next stage
+        up.fuse = 1;
+        up.dnext = derived_out<R>(h, nb);
+        up.ph = h->phys;
+    }
     const int quirk = h->p.quirk_dissipation_y != 0;
     if constexpr (std::is_same<R, float>::value)
         launch_rhs_fp32(h->p.stencil_size, h->p.stencil_visc, h->geom, h->phys, h->cf32, rhs_in<float>(h), up, h->scal,
@@ -189,13 +215,20 @@ int rhs_phase(cns_solver* h, int kind, double a, double b) {
                         h->scal, quirk, h->stream);
     h->launches += 1;
     CKL();
-    if (kind != ST_RHS_ONLY) h->cur = nb;
+    if (kind != ST_RHS_ONLY) {
+        // in the reference's program order the latest state recovery before the next
+        // step's time-step reduction is that of this stage's input state
+        h->mu_buf = h->cur;
+        h->der_ok[nb] = true;
+        h->cur = nb;
+    }
     return CNS_OK;
 }
 
-int state_any(cns_solver* h, int adv, double* tl) {
-    return h->fp32 ? state_phase<float>(h, adv, tl) : state_phase<double>(h, adv, tl);
-}
+int state_any(cns_solver* h) { return h->fp32 ? state_phase<float>(h) : state_phase<double>(h); }
+int ghost_any(cns_solver* h) { return h->fp32 ? ghost_phase<float>(h) : ghost_phase<double>(h); }
+// the derived fields of the current state, recovered unless the last stage did it
+int ensure_state(cns_solver* h) { return h->der_ok[h->cur] ? CNS_OK : state_any(h); }
 int grad_any(cns_solver* h) { return h->fp32 ? grad_phase<float>(h) : grad_phase<double>(h); }
 int rhs_any(cns_solver* h, int kind, double a, double b) {
     return h->fp32 ? rhs_phase<float>(h, kind, a, b) : rhs_phase<double>(h, kind, a, b);
@@ -204,9 +237,9 @@ int rhs_any(cns_solver* h, int kind, double a, double b) {
 }  // namespace
 
 int cns::solver_reduce(cns_solver* h, int want, double* diag) {
-    if (h->fp32) launch_reduce<float>(h->geom, h->phys, state_in(h, h->cur), (const float*)h->der[3], h->part, want,
+    if (h->fp32) launch_reduce<float>(h->geom, h->phys, state_in(h, h->cur), (const float*)h->der[h->mu_buf][3], h->part, want,
                                       h->scal, diag, h->stream);
-    else launch_reduce<double>(h->geom, h->phys, state_in(h, h->cur), (const double*)h->der[3], h->part, want,
+    else launch_reduce<double>(h->geom, h->phys, state_in(h, h->cur), (const double*)h->der[h->mu_buf][3], h->part, want,
                                h->scal, diag, h->stream);
     h->launches += 2;
     CKL();
@@ -223,8 +256,14 @@ int step_stages(cns_solver* h, double* time_log) {
     int rc;
     const int sch = h->p.scheme;
     const int nst = sch == CNS_RK4_CLASSIC ? 4 : 3;
+    // the state recovery of each stage's input comes from the previous stage's RHS kernel
+    // (ensure_state before the first step)
     for (int s = 0; s < nst; s++) {
-        if ((rc = state_any(h, s == 0, s == 0 ? time_log : nullptr))) return rc;
+        if (s == 0) {
+            launch_advance_time(h->scal, time_log, h->diag_cap, h->stream);
+            h->launches += 1;
+        }
+        if ((rc = ghost_any(h))) return rc;
         if ((rc = grad_any(h))) return rc;
         int kind;
         double a = 0, b = 0;
@@ -266,7 +305,11 @@ int step_graph(cns_solver* h) {
 
 }  // namespace
 
-int cns::solver_step(cns_solver* h) { return h->use_graphs ? step_graph(h) : step_stages(h, h->tlog); }
+int cns::solver_step(cns_solver* h) {
+    const int rc = ensure_state(h);
+    if (rc) return rc;
+    return h->use_graphs ? step_graph(h) : step_stages(h, h->tlog);
+}
 
 namespace {
 
@@ -413,9 +456,11 @@ int cns_create(const cns_params* pin, int device, cns_solver** out) {
     const size_t N = (size_t)p.mx * p.my * p.mz;
     for (int b = 0; b < 2 && !rc; b++)
         for (int f = 0; f < 5 && !rc; f++) rc = h->alloc_field((void**)&h->q[b][f], 8);
-    for (int f = 0; f < 4 && !rc; f++) rc = h->alloc_field(&h->der[f], rs);
-    if (!rc && h->fp32)
-        for (int f = 0; f < 4 && !rc; f++) rc = h->alloc_field(&h->s32[f], 4);
+    for (int b = 0; b < 2; b++) {
+        for (int f = 0; f < 4 && !rc; f++) rc = h->alloc_field(&h->der[b][f], rs);
+        if (!rc && h->fp32)
+            for (int f = 0; f < 4 && !rc; f++) rc = h->alloc_field(&h->s32[b][f], 4);
+    }
     if (!rc) rc = h->alloc_field(&h->dil, rs);
     for (int f = 0; f < 9 && !rc; f++) rc = h->alloc_field(&h->grad[f], rs);
     for (int f = 0; f < 5 && !rc; f++) rc = h->alloc_field(&h->rb[f], rs);
@@ -563,7 +608,8 @@ int cns_copy_field(cns_solver* h, int direction, double* r, double* u, double* v
             h->launches++;
         }
         CKL();
-        int rc = state_any(h, 0, nullptr);   // calcState (copyField(0), src/cuda_utils.cu:331-332)
+        h->der_ok[0] = h->der_ok[1] = false;
+        int rc = state_any(h);   // calcState (copyField(0), src/cuda_utils.cu:331-332)
         if (rc) return rc;
         h->initialized = true;
         return sync_and_check(h);
@@ -598,6 +644,7 @@ int cns_run(cns_solver* h, int nsteps, double* par1, double* par2, double* time)
         h->drop_graphs();
     }
     CK(cudaMemsetAsync(h->scal + SC_STEP, 0, sizeof(double), h->stream));   // step counter of this run
+    if ((rc = ensure_state(h))) return rc;   // outside any captured step graph
     const int forcing = h->p.forcing != 0;
     for (int s = 0; s < nsteps; s++) {
         int want = 0;
@@ -639,7 +686,8 @@ int cns_calc_rhs(cns_solver* h, double* rr, double* ru, double* rv, double* rw, 
     double* out[5] = {rr, ru, rv, rw, re};
     CK(cudaSetDevice(h->device));
     int rc;
-    if ((rc = state_any(h, 0, nullptr)) || (rc = grad_any(h)) || (rc = rhs_any(h, ST_RHS_ONLY, 0, 0))) return rc;
+    if ((rc = state_any(h)) || (rc = ghost_any(h)) || (rc = grad_any(h)) || (rc = rhs_any(h, ST_RHS_ONLY, 0, 0)))
+        return rc;
     const size_t N = (size_t)h->p.mx * h->p.my * h->p.mz;
     for (int f = 0; f < 5; f++) {
         if (h->fp32) launch_pack<float>(h->geom, (const float*)h->rb[f], h->staging, h->stream);
@@ -683,11 +731,11 @@ int cns_time_phases(cns_solver* h, int nstages, double* ms) {
     cudaEvent_t ev[4];
     for (int i = 0; i < 4; i++) CK(cudaEventCreate(&ev[i]));
     double acc[3] = {0, 0, 0};
-    int rc = CNS_OK;
+    int rc = ensure_state(h);
     for (int s = 0; s < nstages && !rc; s++) {
         const int st = s % 3;
         CK(cudaEventRecord(ev[0], h->stream));
-        if ((rc = state_any(h, 0, nullptr))) break;
+        if ((rc = ghost_any(h))) break;
         CK(cudaEventRecord(ev[1], h->stream));
         if ((rc = grad_any(h))) break;
         CK(cudaEventRecord(ev[2], h->stream));

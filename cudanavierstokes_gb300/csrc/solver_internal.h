@@ -35,8 +35,14 @@ struct cns_solver {
 
     double* q[2][5] = {};        // state ping-pong (rho, u, v, w, rhoE)
     int cur = 0;
-    void* der[4] = {};           // h, t, p, mu   (R)
-    void* s32[4] = {};           // FP32 stencil copies of rho, u, v, w
+    // derived fields h, t, p, mu (R) and the FP32 stencil copies of rho, u, v, w of the
+    // state buffer q[b], in der[b] / s32[b]: the RHS kernel reads those of q[cur] and writes
+    // those of the new state q[1 - cur] (fused state recovery)
+    void* der[2][4] = {};
+    void* s32[2][4] = {};
+    bool der_ok[2] = {false, false};   // der[b] / s32[b] hold the recovery of q[b]
+    int mu_buf = 0;                    // buffer of the latest state recovery in program order of
+                                       // the reference (its mu sets the CFL time step)
     void* dil = nullptr;         // (R)
     void* grad[9] = {};          // (R)
     void* rb[5] = {};            // RHS register (R)
@@ -111,6 +117,14 @@ inline void solver_set_parity(cns_solver* h, int want) {
         h->q[0][f] = h->q[1][f];
         h->q[1][f] = t;
     }
+    for (int f = 0; f < 4; f++) {
+        void* a = h->der[0][f]; h->der[0][f] = h->der[1][f]; h->der[1][f] = a;
+        void* b = h->s32[0][f]; h->s32[0][f] = h->s32[1][f]; h->s32[1][f] = b;
+    }
+    const bool ok0 = h->der_ok[0];
+    h->der_ok[0] = h->der_ok[1];
+    h->der_ok[1] = ok0;
+    h->mu_buf = 1 - h->mu_buf;
     h->cur = want;
     h->drop_graphs();
 }

@@ -191,9 +191,10 @@ CNS_API int cns_get_scalars(cns_solver* h, double* dt, double* dpdz, double* tim
 CNS_API int cns_set_scalars(cns_solver* h, double dt, double dpdz, double time, int64_t step);
 
 /* Time `nstages` Runge-Kutta stages (low-storage coefficients, the state advances) phase
- * by phase with CUDA events on the handle's stream. ms[0]: state recovery + ghost fill,
- * ms[1]: velocity gradients + dilatation ghosts, ms[2]: the RHS + stage-update kernel;
- * averages per stage. No counterpart in the reference (it has no timers, src/main.cpp:71-75). */
+ * by phase with CUDA events on the handle's stream. ms[0]: ghost fill of the stencil
+ * inputs, ms[1]: velocity gradients + dilatation ghosts, ms[2]: the RHS + stage-update
+ * kernel, which also recovers T, p, H, mu of the new state for the next stage; averages
+ * per stage. No counterpart in the reference (it has no timers, src/main.cpp:71-75). */
 CNS_API int cns_time_phases(cns_solver* h, int nstages, double* ms);
 
 /* Number of CUDA kernels this handle has launched since creation. */
