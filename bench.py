@@ -423,7 +423,7 @@ def run_gb300(args, world, rank, local):
     ph = s.time_phases(6)
     S, V = p.stencil_size, p.stencil_visc
     rhs_s = ph["rhs_ms"] * 1e-3
-    ach_tf = rf.rhs_kernel_flops(S, V) * N / rhs_s / 1e12
+    ach_tf = rf.fused_rhs_kernel_flops(S, V) * N / rhs_s / 1e12
     ach_gbs = rf.RHS_KERNEL_BYTES * N / rhs_s / 1e9
     t64 = native.ctypes.c_double()
     native.check(native.lib().cns_probe_fma_peak(local, 1 if args.precision == "fp64" else 0,
@@ -440,7 +440,7 @@ def run_gb300(args, world, rank, local):
             "sponge + RK stage update)", "achieved": ach_tf, "peak": t64.value, "unit": "TFLOP/s",
             "frac": ach_tf / t64.value, "peak_source": "measured live (FMA-chain probe, cns_probe_fma_peak)",
             "traffic": traffic, "launch_ms": ph["rhs_ms"],
-            "flops_per_point": rf.rhs_kernel_flops(S, V), "bytes_per_point": rf.RHS_KERNEL_BYTES,
+            "flops_per_point": rf.fused_rhs_kernel_flops(S, V), "bytes_per_point": rf.RHS_KERNEL_BYTES,
             "hbm": {"achieved": ach_gbs, "peak": hbm_peak, "unit": "GB/s", "frac": ach_gbs / hbm_peak,
                     "peak_source": hbm_src},
             "phase_ms": ph}

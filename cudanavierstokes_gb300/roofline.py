@@ -25,6 +25,11 @@ def grad_kernel_flops(V: int) -> float:
     return 9 * (3 * V + 1) + 2
 
 
+def fused_rhs_kernel_flops(S: int, V: int) -> float:
+    """The RHS kernel also recovers the next stage's state (calcState's arithmetic)."""
+    return rhs_kernel_flops(S, V) + state_kernel_flops()
+
+
 def state_kernel_flops() -> float:
     return 14.0
 
