@@ -3,9 +3,10 @@
 // One handle = one simulation resident on one GPU. A time step is
 //   [every check_cfl / check_bulk steps: one fused two-pass reduction for dt, the body
 //    force controller and the bulk diagnostics, all on the device]
-//   then per Runge-Kutta stage:
-//     k_state (T, p, H, mu, lambda) -> k_ghost_state -> k_grad (9 gradients + theta)
-//     -> k_ghost_scalar (theta) -> k_rhs (RHS of x, y, z + body force + sponge + update)
+//   k_advance_time, then per Runge-Kutta stage:
+//     k_ghost_state -> k_grad (9 gradients + theta) -> k_ghost_scalar (theta)
+//     -> k_rhs (RHS of x, y, z + body force + sponge + update, and T, p, H, mu of the new
+//        state for the next stage; k_state runs only after the state is set from outside)
 // with no host round trip inside a run (the reference copies dt and dpdz through the
 // host and MPI every check_cfl steps: src/cuda_main.cu:249-265).
 #include <cuda_runtime.h>
