@@ -106,3 +106,58 @@ def test_driver_matches_library_and_restarts(tmp_path, gpu_lib):
     # the restart continues the clock from the saved scalars
     t_full = (tmp_path / "fields" / "scalars.0000002.txt").read_text()
     assert (out_dir / "fields" / "scalars.0000002.txt").read_text() == t_full
+
+
+BL_PARAMS = """# boundary layer from generated self-similar inflow profiles
+mx_tot = 16
+my_tot = 8
+mz_tot = 160
+Lx = 20.0
+Ly = 7.0
+Lz = 100.0
+stencilSize = 3
+stencilVisc = 2
+nsteps = 3
+nfiles = 1
+restartFile = -1
+CFL = 0.75
+Re = 1500.0
+Pr = 0.75
+Ma = 0.35
+viscexp = 1.5
+gam = 1.4
+boundaryLayer = 1
+perturbed = 1
+periodicX = 0
+nonUniformX = 1
+stretch = 5.0
+checkCFLcondition = 1
+checkBulk = 1
+"""
+
+
+@pytest.mark.gpu
+def test_driver_boundary_layer_from_generated_profiles(tmp_path, gpu_lib, oracle_mod):
+    """The driver's boundary-layer start (sponge references from blasius1D/*.bin, which
+    cudanavierstokes_gb300.blasius writes) and three steps, against the oracle."""
+    pytest.importorskip("scipy")
+    from cudanavierstokes_gb300.blasius import self_similar_profiles, write_profiles
+    from cudanavierstokes_gb300.params import boundary_layer_params
+    from tests._util import state_errors
+    build.build()
+    p = boundary_layer_params(16, 8, 160).copy(check_cfl=1, check_bulk=1)   # as the parameter file
+    prof = self_similar_profiles(p.gam, p.Ma, p.Pr)
+    write_profiles(str(tmp_path), prof)
+    pf = tmp_path / "params.txt"
+    pf.write_text(BL_PARAMS)
+    r = subprocess.run([build.DRIVER, str(pf), str(tmp_path)], capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0, r.stderr
+    o = oracle_mod.Oracle(p)
+    spx, spz = o.sponge_strengths()
+    args = [prof[k] for k in ("x", "r", "u", "w", "e")]
+    rref, uref, wref, eref = o.sponge_refs(*args)
+    o.set_sponge(spx, spz, rref, uref, wref, eref)
+    o.set_state(*[np.broadcast_to(a[:, None, :], p.shape).copy() for a in (rref, uref, np.zeros_like(rref), wref, eref)])
+    np.testing.assert_array_equal(read_fields(str(tmp_path / "fields"), 0, p.shape)[0], o.get_state()[0])
+    o.run(3)
+    assert max(state_errors(read_fields(str(tmp_path / "fields"), 1, p.shape), o.get_state())) <= 1e-12
