@@ -339,8 +339,11 @@ __device__ __forceinline__ void rhs_point(const Geom& g, const CoefT<R>& cf, con
     rhs_point_nb<R, S, V>(g, cf, in, up, scal, quirk, i, k, c, nx, ny, nz, th0, m0, u0, v0, w0, r0, h0);
 }
 
+// FP32: 7 blocks of 128 per SM (72 registers) measured fastest (6: 80 registers, +13 %
+// time; 5: 96 registers, and stages that read the RK register ran 3.5x slower); FP64: the
+// FP64 pipe bounds the kernel at 3 to 5 blocks alike
 template <typename R, int S, int V>
-__global__ void __launch_bounds__(128, sizeof(R) == 4 ? 6 : 4) k_rhs(Geom g, CoefT<R> cf, RhsIn<R> in, Update<R> up,
+__global__ void __launch_bounds__(128, sizeof(R) == 4 ? 7 : 4) k_rhs(Geom g, CoefT<R> cf, RhsIn<R> in, Update<R> up,
                                              double* __restrict__ scal, int quirk) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     const int j = blockIdx.y * blockDim.y + threadIdx.y;

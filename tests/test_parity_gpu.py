@@ -278,3 +278,16 @@ def test_graph_replay_matches_direct_launches(gpu_lib):
     for k in ("par1", "time"):
         np.testing.assert_array_equal(logs[0][k], logs[2][k])
         np.testing.assert_array_equal(logs[1][k], logs[3][k])
+
+
+def test_fp32_rhs_stage_kinds_run_alike(gpu_lib):
+    """Performance guard: a Wray stage that reads the previous RHS (a != 0) must not be much
+    slower than the first stage (interleaved register loads and stores once made the
+    kernel 3.7x slower for those stages)."""
+    p = channel_params(128, 160, 48, precision=PREC_FP32_RHS)
+    s = Solver(p)
+    s.copy_field_in(*channel_fields(p, s.grid()["x"], seed=0))
+    s.time_phases(3)
+    first = min(s.time_phases(1)["rhs_ms"] for _ in range(3))
+    avg = min(s.time_phases(3)["rhs_ms"] for _ in range(3))
+    assert avg <= 1.5 * first, (first, avg)
