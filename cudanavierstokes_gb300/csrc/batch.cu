@@ -138,7 +138,9 @@ int64_t estimate_bytes(const cns_params& p, int64_t log_steps) {
     const long long nall = P * (p.my + 2 * G) * (p.mz + 2 * G);
     const bool f32 = p.precision == CNS_PREC_FP32_RHS;
     const long long rs = f32 ? 4 : 8;
-    long long bytes = 10 * nall * 8 + (5 + 1 + 9 + 5) * nall * rs + (f32 ? 4 * nall * 4 : 0);
+    // 2 x 5 FP64 state; derived h, t, p, mu of both state buffers, theta, 5 RK register
+    // fields and (FP64) 9 velocity gradients in the RHS type; FP32: 2 x 4 stencil copies
+    long long bytes = 10 * nall * 8 + (8 + 1 + 5 + (f32 ? 0 : 9)) * nall * rs + (f32 ? 8 * nall * 4 : 0);
     bytes += (long long)p.mx * p.my * p.mz * 8;   // staging
     bytes += 3 * 8 * (int64_t)std::max<int64_t>(log_steps, 1024) + 64 * 1024;
     return bytes;

@@ -138,7 +138,7 @@ __global__ void __launch_bounds__(256, sizeof(R) == 4 ? 2 : 1) k_batch_stage(con
             GradOut<R> go;
             for (int c = 0; c < 9; c++) go.g[c] = I.grad[c];
             go.dil = I.dil;
-            grad_point<R, V>(I.g, I.cf, uu, vv, ww, go, i, j, k);
+            grad_point<R, V, sizeof(R) == 4>(I.g, I.cf, uu, vv, ww, go, i, j, k);
         }
     }
     grid_barrier(bar, nb, err);

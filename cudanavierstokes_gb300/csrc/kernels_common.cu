@@ -35,7 +35,7 @@ __global__ void __launch_bounds__(128) k_grad(Geom g, CoefT<R> cf, const R* __re
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     const int j = blockIdx.y * blockDim.y + threadIdx.y;
     if (i >= g.mx || j >= g.my) return;
-    grad_point<R, V>(g, cf, u, v, w, o, i, j, (int)blockIdx.z);
+    grad_point<R, V, sizeof(R) == 4>(g, cf, u, v, w, o, i, j, (int)blockIdx.z);
 }
 
 template <typename R>

@@ -165,7 +165,9 @@ __device__ __forceinline__ void ghost_state_cell(const Geom& g, const Phys& ph, 
 // Velocity gradients gij[0..8] = d(u,v,w)/d(x,y,z) at the viscous order and the
 // dilatation (derVelX/Y/Z + calcDil, src/calc_stress.cu:20-63,87-96).
 // ---------------------------------------------------------------------------------
-template <typename R, int V>
+// DIL_ONLY: only the three diagonal gradients and theta (the FP32-RHS kernel forms the nine
+// gradients itself from the velocity stencils it loads, and needs theta at its neighbours)
+template <typename R, int V, bool DIL_ONLY = false>
 __device__ __forceinline__ void grad_point(const Geom& g, const CoefT<R>& cf, const R* __restrict__ u,
                                            const R* __restrict__ v, const R* __restrict__ w, const GradOut<R>& o,
                                            int i, int j, int k) {
@@ -177,6 +179,7 @@ __device__ __forceinline__ void grad_point(const Geom& g, const CoefT<R>& cf, co
     for (int d = 0; d < 3; d++) {
 #pragma unroll
         for (int q = 0; q < 3; q++) {
+            if (DIL_ONLY && q != d) continue;
             const R* f = F[q];
             R s = cf.c1V[d][1] * (__ldg(f + c + st[d]) - __ldg(f + c - st[d]));
 #pragma unroll
@@ -186,8 +189,10 @@ __device__ __forceinline__ void grad_point(const Geom& g, const CoefT<R>& cf, co
             out[3 * d + q] = s;
         }
     }
+    if constexpr (!DIL_ONLY) {
 #pragma unroll
-    for (int q = 0; q < 9; q++) o.g[q][c] = out[q];
+        for (int q = 0; q < 9; q++) o.g[q][c] = out[q];
+    }
     o.dil[c] = out[0] + out[4] + out[8];
 }
 

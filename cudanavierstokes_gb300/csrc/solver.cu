@@ -463,7 +463,8 @@ int cns_create(const cns_params* pin, int device, cns_solver** out) {
             for (int f = 0; f < 4 && !rc; f++) rc = h->alloc_field(&h->s32[b][f], 4);
     }
     if (!rc) rc = h->alloc_field(&h->dil, rs);
-    for (int f = 0; f < 9 && !rc; f++) rc = h->alloc_field(&h->grad[f], rs);
+    if (!h->fp32)   // FP32-RHS: the RHS kernel forms the velocity gradients itself
+        for (int f = 0; f < 9 && !rc; f++) rc = h->alloc_field(&h->grad[f], rs);
     for (int f = 0; f < 5 && !rc; f++) rc = h->alloc_field(&h->rb[f], rs);
     if (!rc && p.scheme != CNS_RK3_LOWSTORAGE) {
         for (int f = 0; f < 5 && !rc; f++) rc = h->alloc_field(&h->k2[f], rs);
