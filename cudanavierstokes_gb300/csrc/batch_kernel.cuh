@@ -120,7 +120,7 @@ __global__ void __launch_bounds__(256, sizeof(R) == 4 ? 2 : 1) k_batch_stage(con
                 f.r = (R*)I.q[cur][0]; f.u = (R*)I.q[cur][1]; f.v = (R*)I.q[cur][2]; f.w = (R*)I.q[cur][3];
             }
             f.h = I.der[0]; f.t = I.der[1]; f.p = I.der[2]; f.m = I.der[3];
-            ghost_state_cell<R>(I.g, I.ph, f, I.scal, t);
+            ghost_state_cell<R>(I.g, I.ph, f, I.scal, (int)t);
         }
     }
     grid_barrier(bar, nb, err);
@@ -147,7 +147,7 @@ __global__ void __launch_bounds__(256, sizeof(R) == 4 ? 2 : 1) k_batch_stage(con
         const int q = find_inst(ctl->ghost_off, n, u);
         const BatchInst<R>& I = tab[q];
         const long long t = (u - ctl->ghost_off[q]) * blockDim.x + threadIdx.x;
-        if (t < ghost_count(I.g)) ghost_scalar_cell<R>(I.g, I.dil, t);
+        if (t < ghost_count(I.g)) ghost_scalar_cell<R>(I.g, I.dil, (int)t);
     }
     grid_barrier(bar, nb, err);
     // phase 5: RHS + stage update into the other state buffer. The unit's x-y neighbourhood

@@ -25,7 +25,7 @@ __global__ void k_advance_time(double* scal, double* time_log, long long tcap) {
 
 template <typename R>
 __global__ void __launch_bounds__(256) k_ghost_state(Geom g, Phys ph, StencilFields<R> f, const double* scal) {
-    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const int t = (int)(blockIdx.x * blockDim.x + threadIdx.x);
     if (t < ghost_count(g)) ghost_state_cell<R>(g, ph, f, scal, t);
 }
 
@@ -40,7 +40,7 @@ __global__ void __launch_bounds__(128) k_grad(Geom g, CoefT<R> cf, const R* __re
 
 template <typename R>
 __global__ void __launch_bounds__(256) k_ghost_scalar(Geom g, R* f) {
-    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const int t = (int)(blockIdx.x * blockDim.x + threadIdx.x);
     if (t < ghost_count(g)) ghost_scalar_cell<R>(g, f, t);
 }
 

@@ -71,6 +71,44 @@ __host__ __device__ __forceinline__ long long ghost_count(const Geom& g) {
     return 2 * G * ((long long)g.my * g.mz + (long long)g.mx * g.mz + (long long)g.mx * g.my);
 }
 
+// Ghost cell numbering shared by the state and dilatation fills: x faces first (m, the
+// distance from the face, fastest, then side, j, k), then the y faces and the z faces with i
+// fastest (then m, side and k or j), so that a warp's loads and stores on the y and z faces
+// are row segments. 32-bit arithmetic: the ghost count is below the padded field size,
+// itself below 2^31.
+struct GhostCell {
+    int face;       // 0 x, 1 y, 2 z
+    int m;          // 1..G, distance of the ghost from the boundary node
+    int side;       // 0 low, 1 high
+    int i, j, k;    // the two in-face indices (the face's own index is unused)
+};
+
+__device__ __forceinline__ GhostCell ghost_cell_of(const Geom& g, int t) {
+    const unsigned G = (unsigned)g.G, mx = (unsigned)g.mx, my = (unsigned)g.my;
+    const unsigned nx = 2u * G * my * (unsigned)g.mz, ny = 2u * G * mx * (unsigned)g.mz;
+    unsigned u = (unsigned)t;
+    GhostCell c;
+    c.i = c.j = c.k = 0;
+    if (u < nx) {
+        c.face = 0;
+        c.m = (int)(u % G) + 1; u /= G;
+        c.side = (int)(u & 1u); u >>= 1;
+        c.j = (int)(u % my);
+        c.k = (int)(u / my);
+        return c;
+    }
+    u -= nx;
+    const bool yf = u < ny;
+    if (!yf) u -= ny;
+    c.face = yf ? 1 : 2;
+    c.i = (int)(u % mx); u /= mx;
+    c.m = (int)(u % G) + 1; u /= G;
+    c.side = (int)(u & 1u); u >>= 1;
+    if (yf) c.k = (int)u;
+    else c.j = (int)u;
+    return c;
+}
+
 // ---------------------------------------------------------------------------------
 // Ghost cell t of the stencil inputs rho, u, v, w, T, p, H, mu.
 //   x: periodic | isothermal wall (BCxNumber1/3: p even, u v w odd, T = 2Tw - T,
@@ -78,87 +116,72 @@ __host__ __device__ __forceinline__ long long ghost_count(const Geom& g) {
 //      even, u v w odd, u perturbed; top: linear extrapolation; mu, rho, H derived)
 //   y: periodic.   z: periodic | linear extrapolation about the end nodes.
 // (src/boundary.h:38-188, src/boundary_condition_x.h:47-115, _y.h:19-58, _z.h:80-332)
-// Only the six faces are filled (no stencil reads an edge or a corner).
+// Only the six faces are filled (no stencil reads an edge or a corner). All loads of a cell
+// are issued before its stores (the eight fields may alias as far as the compiler knows).
 // ---------------------------------------------------------------------------------
 template <typename R>
 __device__ __forceinline__ void ghost_state_cell(const Geom& g, const Phys& ph, const StencilFields<R>& f,
-                                                 const double* scal, long long t) {
-    const long long G = g.G;
-    const long long nx = 2 * G * g.my * g.mz, ny = 2 * G * g.mx * g.mz, nz = 2 * G * g.mx * g.my;
+                                                 const double* scal, int t) {
     R* F[8] = {f.r, f.u, f.v, f.w, f.t, f.p, f.h, f.m};
-    if (t < nx) {
-        const int m = (int)(t % G) + 1; t /= G;
-        const int side = (int)(t % 2); t /= 2;
-        const int j = (int)(t % g.my);
-        const int k = (int)(t / g.my);
-        const int ig = side == 0 ? -m : g.mx - 1 + m;
-        const long long cg = g.at(ig, j, k);
-        if (g.xbc == XBC_PER) {
-            const long long cs = g.at(side == 0 ? g.mx - m : m - 1, j, k);
-#pragma unroll
-            for (int q = 0; q < 8; q++) F[q][cg] = F[q][cs];
+    const GhostCell gc = ghost_cell_of(g, t);
+    const int m = gc.m, side = gc.side;
+    long long cg, cs;
+    if (gc.face == 0) {
+        const int j = gc.j, k = gc.k;
+        cg = g.at(side == 0 ? -m : g.mx - 1 + m, j, k);
+        if (g.xbc != XBC_PER) {
+            const long long cp = g.at(side == 0 ? m - 1 : g.mx - m, j, k);
+            R ug, vg, wg, pg, Tg;
+            if (g.xbc == XBC_WALL) {
+                const double Tw = side == 0 ? ph.twall_bot : ph.twall_top;
+                ug = -f.u[cp]; vg = -f.v[cp]; wg = -f.w[cp];
+                pg = f.p[cp];
+                Tg = (R)(2.0 * Tw) - f.t[cp];
+            } else if (side == 0) {   // boundary layer, wall
+                ug = -f.u[cp]; vg = -f.v[cp]; wg = -f.w[cp];
+                pg = f.p[cp];
+                Tg = f.t[cp];
+                double pv;
+                if (ph.perturbed && wall_perturbation(ph, g.dy, j, k, scal[SC_TIME], &pv)) ug = to_r<R>(pv);
+            } else {                  // boundary layer, free stream: extrapolate through the last node
+                const long long cl = g.at(g.mx - 1, j, k);
+                const long long cm = g.at(g.mx - 1 - m, j, k);
+                ug = (R)2.0 * f.u[cl] - f.u[cm];
+                vg = (R)2.0 * f.v[cl] - f.v[cm];
+                wg = (R)2.0 * f.w[cl] - f.w[cm];
+                pg = (R)2.0 * f.p[cl] - f.p[cm];
+                Tg = (R)2.0 * f.t[cl] - f.t[cm];
+            }
+            const R suth = ph.vexp_is_one ? Tg : cns_pow<R>(Tg, (R)ph.vexp);
+            f.u[cg] = ug; f.v[cg] = vg; f.w[cg] = wg; f.p[cg] = pg; f.t[cg] = Tg;
+            f.m[cg] = suth * (R)ph.invRe;
+            f.h[cg] = Tg * (R)ph.hcoef + (R)0.5 * (ug * ug + vg * vg + wg * wg);
+            f.r[cg] = pg / ((R)ph.Rgas * Tg);
             return;
         }
-        const int ip = side == 0 ? m - 1 : g.mx - m;
-        const long long cp = g.at(ip, j, k);
-        R ug, vg, wg, pg, Tg;
-        if (g.xbc == XBC_WALL) {
-            const double Tw = side == 0 ? ph.twall_bot : ph.twall_top;
-            ug = -f.u[cp]; vg = -f.v[cp]; wg = -f.w[cp];
-            pg = f.p[cp];
-            Tg = (R)(2.0 * Tw) - f.t[cp];
-        } else if (side == 0) {   // boundary layer, wall
-            ug = -f.u[cp]; vg = -f.v[cp]; wg = -f.w[cp];
-            pg = f.p[cp];
-            Tg = f.t[cp];
-            double pv;
-            if (ph.perturbed && wall_perturbation(ph, g.dy, j, k, scal[SC_TIME], &pv)) ug = to_r<R>(pv);
-        } else {                  // boundary layer, free stream: extrapolate through the last node
-            const long long cl = g.at(g.mx - 1, j, k);
-            const long long cm = g.at(g.mx - 1 - m, j, k);
-            ug = (R)2.0 * f.u[cl] - f.u[cm];
-            vg = (R)2.0 * f.v[cl] - f.v[cm];
-            wg = (R)2.0 * f.w[cl] - f.w[cm];
-            pg = (R)2.0 * f.p[cl] - f.p[cm];
-            Tg = (R)2.0 * f.t[cl] - f.t[cm];
+        cs = g.at(side == 0 ? g.mx - m : m - 1, j, k);
+    } else if (gc.face == 1) {
+        cg = g.at(gc.i, side == 0 ? -m : g.my - 1 + m, gc.k);
+        cs = g.at(gc.i, side == 0 ? g.my - m : m - 1, gc.k);
+    } else {
+        cg = g.at(gc.i, gc.j, side == 0 ? -m : g.mz - 1 + m);
+        if (g.zbl) {
+            const long long c0 = g.at(gc.i, gc.j, side == 0 ? 0 : g.mz - 1);
+            const long long cm = g.at(gc.i, gc.j, side == 0 ? m : g.mz - 1 - m);
+            R a[8], b[8];
+#pragma unroll
+            for (int q = 0; q < 8; q++) { a[q] = F[q][c0]; b[q] = F[q][cm]; }
+#pragma unroll
+            for (int q = 0; q < 8; q++) F[q][cg] = (R)2.0 * a[q] - b[q];
+            return;
         }
-        const R suth = ph.vexp_is_one ? Tg : cns_pow<R>(Tg, (R)ph.vexp);
-        f.u[cg] = ug; f.v[cg] = vg; f.w[cg] = wg; f.p[cg] = pg; f.t[cg] = Tg;
-        f.m[cg] = suth * (R)ph.invRe;
-        f.h[cg] = Tg * (R)ph.hcoef + (R)0.5 * (ug * ug + vg * vg + wg * wg);
-        f.r[cg] = pg / ((R)ph.Rgas * Tg);
-        return;
+        cs = g.at(gc.i, gc.j, side == 0 ? g.mz - m : m - 1);
     }
-    t -= nx;
-    if (t < ny) {
-        const int m = (int)(t % G) + 1; t /= G;
-        const int side = (int)(t % 2); t /= 2;
-        const int i = (int)(t % g.mx);
-        const int k = (int)(t / g.mx);
-        const long long cg = g.at(i, side == 0 ? -m : g.my - 1 + m, k);
-        const long long cs = g.at(i, side == 0 ? g.my - m : m - 1, k);
+    R v[8];
 #pragma unroll
-        for (int q = 0; q < 8; q++) F[q][cg] = F[q][cs];
-        return;
-    }
-    t -= ny;
-    if (t < nz) {
-        const int m = (int)(t % G) + 1; t /= G;
-        const int side = (int)(t % 2); t /= 2;
-        const int i = (int)(t % g.mx);
-        const int j = (int)(t / g.mx);
-        const long long cg = g.at(i, j, side == 0 ? -m : g.mz - 1 + m);
-        if (!g.zbl) {
-            const long long cs = g.at(i, j, side == 0 ? g.mz - m : m - 1);
+    for (int q = 0; q < 8; q++) v[q] = F[q][cs];
 #pragma unroll
-            for (int q = 0; q < 8; q++) F[q][cg] = F[q][cs];
-        } else {
-            const long long c0 = g.at(i, j, side == 0 ? 0 : g.mz - 1);
-            const long long cm = g.at(i, j, side == 0 ? m : g.mz - 1 - m);
-#pragma unroll
-            for (int q = 0; q < 8; q++) F[q][cg] = (R)2.0 * F[q][c0] - F[q][cm];
-        }
-    }
+    for (int q = 0; q < 8; q++) F[q][cg] = v[q];
 }
 
 // ---------------------------------------------------------------------------------
@@ -199,35 +222,19 @@ __device__ __forceinline__ void grad_point(const Geom& g, const CoefT<R>& cf, co
 // Dilatation ghost cell t (BCxNumber2 / BCyNumber1 / BCzNumber1): x periodic | wall:
 // even | boundary layer: bottom even, top extrapolated; y periodic; z periodic | extrapolated.
 template <typename R>
-__device__ __forceinline__ void ghost_scalar_cell(const Geom& g, R* f, long long t) {
-    const long long G = g.G;
-    const long long nx = 2 * G * g.my * g.mz, ny = 2 * G * g.mx * g.mz, nz = 2 * G * g.mx * g.my;
-    if (t < nx) {
-        const int m = (int)(t % G) + 1; t /= G;
-        const int side = (int)(t % 2); t /= 2;
-        const int j = (int)(t % g.my);
-        const int k = (int)(t / g.my);
+__device__ __forceinline__ void ghost_scalar_cell(const Geom& g, R* f, int t) {
+    const GhostCell gc = ghost_cell_of(g, t);
+    const int m = gc.m, side = gc.side;
+    if (gc.face == 0) {
+        const int j = gc.j, k = gc.k;
         const long long cg = g.at(side == 0 ? -m : g.mx - 1 + m, j, k);
         if (g.xbc == XBC_PER) f[cg] = f[g.at(side == 0 ? g.mx - m : m - 1, j, k)];
         else if (g.xbc == XBC_WALL || side == 0) f[cg] = f[g.at(side == 0 ? m - 1 : g.mx - m, j, k)];
         else f[cg] = (R)2.0 * f[g.at(g.mx - 1, j, k)] - f[g.at(g.mx - 1 - m, j, k)];
-        return;
-    }
-    t -= nx;
-    if (t < ny) {
-        const int m = (int)(t % G) + 1; t /= G;
-        const int side = (int)(t % 2); t /= 2;
-        const int i = (int)(t % g.mx);
-        const int k = (int)(t / g.mx);
-        f[g.at(i, side == 0 ? -m : g.my - 1 + m, k)] = f[g.at(i, side == 0 ? g.my - m : m - 1, k)];
-        return;
-    }
-    t -= ny;
-    if (t < nz) {
-        const int m = (int)(t % G) + 1; t /= G;
-        const int side = (int)(t % 2); t /= 2;
-        const int i = (int)(t % g.mx);
-        const int j = (int)(t / g.mx);
+    } else if (gc.face == 1) {
+        f[g.at(gc.i, side == 0 ? -m : g.my - 1 + m, gc.k)] = f[g.at(gc.i, side == 0 ? g.my - m : m - 1, gc.k)];
+    } else {
+        const int i = gc.i, j = gc.j;
         const long long cg = g.at(i, j, side == 0 ? -m : g.mz - 1 + m);
         if (!g.zbl) f[cg] = f[g.at(i, j, side == 0 ? g.mz - m : m - 1)];
         else f[cg] = (R)2.0 * f[g.at(i, j, side == 0 ? 0 : g.mz - 1)] - f[g.at(i, j, side == 0 ? m : g.mz - 1 - m)];
