@@ -1,7 +1,8 @@
 // batch.cu -- batched ensemble: many simulations of uneven grid sizes advanced together.
 // Two execution modes, picked with the launch shape by a measuring autotuner:
 //  - persistent: one persistent cooperative launch per Runge-Kutta stage over the work
-//    units of all members, the step captured in a CUDA graph (one per ping-pong parity);
+//    units of all members (and one small launch that advances every member's time at the
+//    step start), the step captured in a CUDA graph (one per ping-pong parity);
 //  - concurrent: every member advances through its own captured step graph (the
 //    standalone stage kernels, coefficients in the launch parameters) on one of up to
 //    CNS_BATCH_LANES streams forked from and joined into the batch stream, so the
@@ -30,13 +31,13 @@
 using namespace cns;
 
 namespace cns {
-void launch_batch_stage_fp64(int S, int V, dim3 grid, dim3 block, const BatchInst<double>* tab, const BatchCtl* ctl,
-                             int cur, int kind, double a, double b, int stage0, int quirk, unsigned* bar, int* err,
-                             cudaStream_t s);
-void launch_batch_stage_fp32(int S, int V, dim3 grid, dim3 block, const BatchInst<float>* tab, const BatchCtl* ctl,
-                             int cur, int kind, double a, double b, int stage0, int quirk, unsigned* bar, int* err,
-                             cudaStream_t s);
-int batch_stage_occupancy(int fp32, int S, int V, int threads, int* blocks_per_sm);
+void launch_batch_stage_fp64(int S, int V, dim3 grid, const BatchInst<double>* tab, const BatchCtl* ctl, int cur,
+                             int stage, int quirk, unsigned* bar, int* err, cudaStream_t s);
+void launch_batch_stage_fp32(int S, int V, dim3 grid, const BatchInst<float>* tab, const BatchCtl* ctl, int cur,
+                             int stage, int quirk, unsigned* bar, int* err, cudaStream_t s);
+void launch_batch_time_fp64(const BatchInst<double>* tab, const BatchCtl* ctl, cudaStream_t s);
+void launch_batch_time_fp32(const BatchInst<float>* tab, const BatchCtl* ctl, cudaStream_t s);
+int batch_stage_occupancy(int fp32, int S, int V, int* blocks_per_sm);
 }  // namespace cns
 
 namespace {
@@ -147,7 +148,7 @@ int64_t estimate_bytes(const cns_params& p, int64_t log_steps) {
 }
 
 template <typename R>
-BatchInst<R> make_inst(cns_solver* h, int rows, int64_t cap) {
+BatchInst<R> make_inst(cns_solver* h, int64_t cap) {
     BatchInst<R> I;
     std::memset(&I, 0, sizeof I);
     I.g = h->geom;
@@ -155,20 +156,12 @@ BatchInst<R> make_inst(cns_solver* h, int rows, int64_t cap) {
     if constexpr (sizeof(R) == 4) I.cf = h->cf32; else I.cf = h->cf64;
     I.scal = h->scal;
     I.tlog = h->tlog;
-    for (int c = 0; c < 2; c++)
-        for (int f = 0; f < 5; f++) I.q[c][f] = h->q[c][f];
-    // the persistent kernel recovers each stage's state itself, into the derived buffer 0
-    for (int f = 0; f < 4; f++) I.der[f] = (R*)h->der[0][f];
-    for (int f = 0; f < 5; f++) I.rb[f] = (R*)h->rb[f];
-    for (int f = 0; f < 4; f++) I.s32[f] = h->fp32 ? (R*)h->s32[0][f] : nullptr;
-    I.dil = (R*)h->dil;
-    for (int f = 0; f < 9; f++) I.grad[f] = (R*)h->grad[f];
-    if (h->has_sponge) {
-        I.spx = h->spx; I.spz = h->spz; I.rref = h->rref; I.uref = h->uref; I.vref = h->vref;
-        I.wref = h->wref; I.eref = h->eref;
+    for (int c = 0; c < 2; c++) {
+        I.in[c] = cns::solver_rhs_in<R>(h, c);
+        for (int st = 0; st < 3; st++) I.up[st][c] = cns::solver_stage_update<R>(h, ST_LS, WA[st], WB[st], c);
     }
     I.nbx = (h->p.mx + 31) / 32;
-    I.nby = (h->p.my + rows - 1) / rows;
+    I.nby = (h->p.my + 3) / 4;
     I.tcap = cap;
     return I;
 }
@@ -176,19 +169,18 @@ BatchInst<R> make_inst(cns_solver* h, int rows, int64_t cap) {
 template <typename R>
 int upload_table(cns_batch* b) {
     const int n = (int)b->members.size();
-    const int rows = b->threads / 32;
     std::vector<BatchInst<R>> tab(std::max(n, 1));
     BatchCtl ctl;
     std::memset(&ctl, 0, sizeof ctl);
     ctl.n = n;
     for (int q = 0; q < n; q++) {
         cns_solver* h = b->members[q].h;
-        tab[q] = make_inst<R>(h, rows, b->members[q].cap);
+        tab[q] = make_inst<R>(h, b->members[q].cap);
         const long long pu = (long long)tab[q].nbx * tab[q].nby * h->p.mz;
         long long gc = 2LL * h->geom.G *
                        ((long long)h->p.my * h->p.mz + (long long)h->p.mx * h->p.mz + (long long)h->p.mx * h->p.my);
         ctl.unit_off[q + 1] = ctl.unit_off[q] + pu;
-        ctl.ghost_off[q + 1] = ctl.ghost_off[q] + (gc + b->threads - 1) / b->threads;
+        ctl.ghost_off[q + 1] = ctl.ghost_off[q] + (gc + BATCH_THREADS - 1) / BATCH_THREADS;
     }
     BCK(cudaMemcpyAsync(b->d_tab, tab.data(), sizeof(BatchInst<R>) * n, cudaMemcpyHostToDevice, b->stream));
     BCK(cudaMemcpyAsync(b->d_ctl, &ctl, sizeof ctl, cudaMemcpyHostToDevice, b->stream));
@@ -202,13 +194,19 @@ int upload(cns_batch* b) {
 }
 
 int launch_stage(cns_batch* b, int s, int cur) {
-    const dim3 grid(b->nsm * b->blocks_per_sm), block(b->threads);
-    if (b->precision == CNS_PREC_FP32_RHS)
-        launch_batch_stage_fp32(b->S, b->V, grid, block, (const BatchInst<float>*)b->d_tab, b->d_ctl, cur, ST_LS, WA[s],
-                                WB[s], s == 0, b->quirk, b->d_bar, b->d_err, b->stream);
+    const dim3 grid(b->nsm * b->blocks_per_sm);
+    const bool f32 = b->precision == CNS_PREC_FP32_RHS;
+    if (s == 0) {   // the step's time advance, before the stage reads the time
+        if (f32) launch_batch_time_fp32((const BatchInst<float>*)b->d_tab, b->d_ctl, b->stream);
+        else launch_batch_time_fp64((const BatchInst<double>*)b->d_tab, b->d_ctl, b->stream);
+        b->launches++;
+    }
+    if (f32)
+        launch_batch_stage_fp32(b->S, b->V, grid, (const BatchInst<float>*)b->d_tab, b->d_ctl, cur, s, b->quirk,
+                                b->d_bar, b->d_err, b->stream);
     else
-        launch_batch_stage_fp64(b->S, b->V, grid, block, (const BatchInst<double>*)b->d_tab, b->d_ctl, cur, ST_LS,
-                                WA[s], WB[s], s == 0, b->quirk, b->d_bar, b->d_err, b->stream);
+        launch_batch_stage_fp64(b->S, b->V, grid, (const BatchInst<double>*)b->d_tab, b->d_ctl, cur, s, b->quirk,
+                                b->d_bar, b->d_err, b->stream);
     b->launches++;
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) {
@@ -237,7 +235,7 @@ int step_stages(cns_batch* b) {
         BCK(e);
     }
     BCK(cudaGraphLaunch(b->exec[c], b->stream));
-    b->launches += 3;
+    b->launches += 4;
     b->cur = c ^ 1;   // three stages: parity flips once per step
     return CNS_OK;
 }
@@ -285,7 +283,7 @@ Member* find_member(cns_batch* b, int id) {
 
 int choose_shape(cns_batch* b) {
     int occ = 0;
-    int rc = batch_stage_occupancy(b->precision == CNS_PREC_FP32_RHS, b->S, b->V, b->threads, &occ);
+    int rc = batch_stage_occupancy(b->precision == CNS_PREC_FP32_RHS, b->S, b->V, &occ);
     if (rc) return rc;
     if (occ < 1) return cns::set_error(CNS_ERR_CUDA, "batch stage kernel cannot be resident");
     if (b->blocks_per_sm > occ) b->blocks_per_sm = occ;
@@ -474,6 +472,9 @@ int cns_batch_step(cns_batch* b, int nsteps) {
         for (auto& m : b->members) {
             cns_solver* h = m.h;
             h->cur = b->cur;
+            // the persistent stages read the current state's derived fields (recovered by
+            // the previous stage, or here after a copy-in or an admission)
+            if (b->mode == CNS_BATCH_PERSISTENT && (rc = cns::solver_ensure_state(h))) return rc;
             int want = 0;
             double* dg = nullptr;
             const int64_t st = m.steps;
@@ -484,14 +485,17 @@ int cns_batch_step(cns_batch* b, int nsteps) {
             }
             if (want && (rc = cns::solver_reduce(h, want, dg))) return rc;
         }
+        const int c0 = b->cur;
         if ((rc = b->mode == CNS_BATCH_CONCURRENT ? step_members(b) : step_stages(b))) return rc;
         for (auto& m : b->members) {
             m.steps++;
             if (b->mode != CNS_BATCH_CONCURRENT) {
-                // derived buffer 0 holds the recovery of the last stage's input state: the
-                // latest one in the reference's order, not that of the current state
-                m.h->der_ok[0] = m.h->der_ok[1] = false;
-                m.h->mu_buf = 0;
+                // as after the standalone fused stages: both derived buffers match their
+                // states, and the latest recovery in the reference's order is that of the
+                // last stage's input state (buffer c0)
+                m.h->der_ok[0] = m.h->der_ok[1] = true;
+                m.h->mu_buf = c0;
+                m.h->cur = b->cur;
             }
         }
     }
@@ -516,8 +520,8 @@ int cns_batch_step(cns_batch* b, int nsteps) {
 }
 
 int cns_batch_set_shape(cns_batch* b, int threads, int blocks_per_sm) {
-    if (!b || (threads != 128 && threads != 256) || blocks_per_sm < 1)
-        return cns::set_error(CNS_ERR_INVALID, "threads must be 128 or 256, blocks_per_sm >= 1");
+    if (!b || threads != BATCH_THREADS || blocks_per_sm < 1)
+        return cns::set_error(CNS_ERR_INVALID, "threads must be 128, blocks_per_sm >= 1");
     b->threads = threads;
     b->blocks_per_sm = blocks_per_sm;
     int rc = choose_shape(b);
@@ -586,11 +590,15 @@ int cns_batch_tune(cns_batch* b, int steps, double* best_ms) {
         return CNS_OK;
     };
     int rc = measure(CNS_BATCH_CONCURRENT, b->threads, b->blocks_per_sm);
-    for (int threads : {128, 256}) {
-        int occ = 0;
-        if (rc || batch_stage_occupancy(b->precision == CNS_PREC_FP32_RHS, b->S, b->V, threads, &occ) || occ < 1)
-            continue;
-        for (int bps = 1; bps <= std::min(occ, 4) && !rc; bps++) rc = measure(CNS_BATCH_PERSISTENT, threads, bps);
+    int occ = 0;
+    if (!rc && !batch_stage_occupancy(b->precision == CNS_PREC_FP32_RHS, b->S, b->V, &occ) && occ >= 1) {
+        // full residency first, then fewer blocks (less barrier traffic, more cache per block)
+        int prev = 0;
+        for (int bps : {occ, occ - 2, occ / 2, 1}) {
+            if (bps < 1 || bps == prev || rc) continue;
+            rc = measure(CNS_BATCH_PERSISTENT, BATCH_THREADS, bps);
+            prev = bps;
+        }
     }
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);

@@ -2,10 +2,12 @@
 #include "batch_launch.cuh"
 
 namespace cns {
-void launch_batch_stage_fp64(int S, int V, dim3 grid, dim3 block, const BatchInst<double>* tab, const BatchCtl* ctl,
-                             int cur, int kind, double a, double b, int stage0, int quirk, unsigned* bar, int* err,
-                             cudaStream_t s) {
-    batch_launch_dispatch<double>(S, V, grid, block, tab, ctl, cur, kind, a, b, stage0, quirk, bar, err, s);
+void launch_batch_stage_fp64(int S, int V, dim3 grid, const BatchInst<double>* tab, const BatchCtl* ctl, int cur,
+                             int stage, int quirk, unsigned* bar, int* err, cudaStream_t s) {
+    batch_launch_dispatch<double>(S, V, grid, tab, ctl, cur, stage, quirk, bar, err, s);
 }
-cudaError_t batch_occ_fp64(int S, int V, int threads, int* nb) { return batch_occ_dispatch<double>(S, V, threads, nb); }
+void launch_batch_time_fp64(const BatchInst<double>* tab, const BatchCtl* ctl, cudaStream_t s) {
+    batch_time_launch<double>(tab, ctl, s);
+}
+cudaError_t batch_occ_fp64(int S, int V, int* nb) { return batch_occ_dispatch<double>(S, V, nb); }
 }  // namespace cns

@@ -2,13 +2,15 @@
 // advances every instance of a batch (many simulations of different grid sizes and
 // physical parameters sharing the stencil orders and the precision).
 //
-// The launch runs the five stage phases (state recovery, ghost fill, velocity
-// gradients, dilatation ghosts, RHS + update) over the work units of all instances, with
-// a grid barrier between phases. Work unit = a 32 x (blockDim/32) tile of one x-y plane
-// of one instance (point phases) or blockDim ghost cells (ghost phases); units of all
-// instances are numbered consecutively (prefix offsets), so uneven grid sizes balance
-// across the persistent blocks. The instance table, the instance count and the offsets
-// live in device memory, so one captured graph serves any membership of the batch.
+// The launch runs the four stage phases (ghost fill of the stencil inputs, velocity
+// gradients / dilatation, dilatation ghosts, RHS + update + the new state's recovery) over
+// the work units of all instances, with a grid barrier between phases. Work unit = a
+// 32 x 4 tile of one x-y plane of one instance (point phases, the standalone RHS kernel's
+// block) or 128 ghost cells (ghost phases); units of all instances are numbered
+// consecutively (prefix offsets), so uneven grid sizes balance across the persistent
+// blocks. The instance table (with each instance's stage updates prepared on the host),
+// the instance count and the offsets live in device memory, so one captured graph serves
+// any membership of the batch.
 #pragma once
 #include "../../include/cns.h"
 #include "cns_common.cuh"
@@ -18,6 +20,8 @@
 
 namespace cns {
 
+constexpr int BATCH_THREADS = 128;   // 32 x 4 points or 128 ghost cells per work unit
+
 template <typename R>
 struct BatchInst {
     Geom g;
@@ -25,15 +29,11 @@ struct BatchInst {
     CoefT<R> cf;
     double* scal;
     double* tlog;
-    long long tcap;     // capacity of tlog
-    double* q[2][5];
-    R* der[4];      // h, t, p, mu
-    R* s32[4];      // FP32 stencil copies of rho, u, v, w (FP32-RHS mode) or nullptr
-    R* dil;
-    R* grad[9];
-    R* rb[5];
-    const double *spx, *spz, *rref, *uref, *vref, *wref, *eref;   // sponge (nullptr without)
-    int nbx, nby;   // units per plane: ceil(mx/32) x ceil(my/rows)
+    long long tcap;          // capacity of tlog
+    RhsIn<R> in[2];          // stencil inputs (+ theta, gradients) of state buffer b
+    Update<R> up[3][2];      // Wray stage s from state buffer b into 1 - b, with the new
+                             // state's recovery (its derived fields of buffer 1 - b)
+    int nbx, nby;            // units per plane: ceil(mx/32) x ceil(my/4)
 };
 
 struct BatchCtl {
@@ -81,131 +81,85 @@ __device__ __forceinline__ int find_inst(const long long* off, int n, long long 
     return lo;
 }
 
+// Stage 0 of a step: every instance's time advances by its dt (before the ghost fill,
+// which reads the time in the boundary-layer wall perturbation)
+template <typename R>
+__global__ void k_batch_time(const BatchInst<R>* __restrict__ tab, const BatchCtl* __restrict__ ctl) {
+    const int q = blockIdx.x * blockDim.x + threadIdx.x;
+    if (q < ctl->n) advance_time(tab[q].scal, tab[q].tlog, tab[q].tcap);
+}
+
+// the (i, j, k) point of thread (tx, ty) in point unit lu of an instance
+template <typename R>
+__device__ __forceinline__ void unit_point(const BatchInst<R>& I, long long lu, int tx, int ty, int& i, int& j,
+                                           int& k) {
+    const long long pl = (long long)I.nbx * I.nby;
+    k = (int)(lu / pl);
+    const int r = (int)(lu - (long long)k * pl);
+    const int by = r / I.nbx, bx = r - by * I.nbx;
+    i = bx * 32 + tx;
+    j = by * 4 + ty;
+}
+
+// FP32: 5 blocks of 128 per SM (96 registers): the instance parameters come from the table in
+// global memory, not the constant bank, and at 7 blocks (72 registers) they spill 700 bytes a
+// thread (measured 1,095 vs 1,498 Mpoint-steps/s on the 48-member ensemble). FP64: 4 blocks.
 template <typename R, int S, int V>
-__global__ void __launch_bounds__(256, sizeof(R) == 4 ? 2 : 1) k_batch_stage(const BatchInst<R>* __restrict__ tab,
-                                                     const BatchCtl* __restrict__ ctl, int cur, int kind, double a,
-                                                     double b, int stage0, int quirk, unsigned* bar, int* err) {
+__global__ void __launch_bounds__(BATCH_THREADS, sizeof(R) == 4 ? 5 : 4)
+    k_batch_stage(const BatchInst<R>* __restrict__ tab, const BatchCtl* __restrict__ ctl, int cur, int stage,
+                  int quirk, unsigned* bar, int* err) {
     const int n = ctl->n;
     if (n <= 0) return;
-    const int rows = blockDim.x >> 5;
     const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
     const long long npu = ctl->unit_off[n], ngu = ctl->ghost_off[n];
     const unsigned nb = gridDim.x;
 
-    // phase 1: state recovery (+ time advance at stage 0)
-    for (long long u = blockIdx.x; u < npu; u += gridDim.x) {
-        const int q = find_inst(ctl->unit_off, n, u);
-        const BatchInst<R>& I = tab[q];
-        const long long lu = u - ctl->unit_off[q];
-        const int bx = (int)(lu % I.nbx), by = (int)((lu / I.nbx) % I.nby), k = (int)(lu / ((long long)I.nbx * I.nby));
-        const int i = bx * 32 + tx, j = by * rows + ty;
-        if (stage0 && lu == 0 && threadIdx.x == 0)
-            advance_time(I.scal, I.tlog, I.tcap);
-        if (i < I.g.mx && j < I.g.my) {
-            DerivedOut<R> o{I.der[0], I.der[1], I.der[2], I.der[3], I.s32[0], I.s32[1], I.s32[2], I.s32[3]};
-            state_point<R>(I.g, I.ph, StateIn{I.q[cur][0], I.q[cur][1], I.q[cur][2], I.q[cur][3], I.q[cur][4]}, o,
-                           I.scal, i, j, k);
-        }
-    }
-    grid_barrier(bar, nb, err);
-    // phase 2: ghost fill of the stencil inputs
+    // phase 1: ghost cells of the stencil inputs of the current state
     for (long long u = blockIdx.x; u < ngu; u += gridDim.x) {
         const int q = find_inst(ctl->ghost_off, n, u);
         const BatchInst<R>& I = tab[q];
-        const long long t = (u - ctl->ghost_off[q]) * blockDim.x + threadIdx.x;
+        const long long t = (u - ctl->ghost_off[q]) * BATCH_THREADS + threadIdx.x;
         if (t < ghost_count(I.g)) {
-            StencilFields<R> f;
-            if (I.s32[0]) { f.r = I.s32[0]; f.u = I.s32[1]; f.v = I.s32[2]; f.w = I.s32[3]; }
-            else {
-                f.r = (R*)I.q[cur][0]; f.u = (R*)I.q[cur][1]; f.v = (R*)I.q[cur][2]; f.w = (R*)I.q[cur][3];
-            }
-            f.h = I.der[0]; f.t = I.der[1]; f.p = I.der[2]; f.m = I.der[3];
+            const RhsIn<R>& in = I.in[cur];
+            const StencilFields<R> f{(R*)in.r, (R*)in.u, (R*)in.v, (R*)in.w, (R*)in.t, (R*)in.p, (R*)in.h,
+                                     (R*)in.m};
             ghost_state_cell<R>(I.g, I.ph, f, I.scal, (int)t);
         }
     }
     grid_barrier(bar, nb, err);
-    // phase 3: velocity gradients and dilatation
+    // phase 2: dilatation (FP32-RHS: the RHS forms the nine gradients itself) or the nine
+    // velocity gradients and the dilatation
     for (long long u = blockIdx.x; u < npu; u += gridDim.x) {
         const int q = find_inst(ctl->unit_off, n, u);
         const BatchInst<R>& I = tab[q];
-        const long long lu = u - ctl->unit_off[q];
-        const int bx = (int)(lu % I.nbx), by = (int)((lu / I.nbx) % I.nby), k = (int)(lu / ((long long)I.nbx * I.nby));
-        const int i = bx * 32 + tx, j = by * rows + ty;
+        int i, j, k;
+        unit_point(I, u - ctl->unit_off[q], tx, ty, i, j, k);
         if (i < I.g.mx && j < I.g.my) {
-            const R* uu = I.s32[0] ? I.s32[1] : (const R*)I.q[cur][1];
-            const R* vv = I.s32[0] ? I.s32[2] : (const R*)I.q[cur][2];
-            const R* ww = I.s32[0] ? I.s32[3] : (const R*)I.q[cur][3];
+            const RhsIn<R>& in = I.in[cur];
             GradOut<R> go;
-            for (int c = 0; c < 9; c++) go.g[c] = I.grad[c];
-            go.dil = I.dil;
-            grad_point<R, V, sizeof(R) == 4>(I.g, I.cf, uu, vv, ww, go, i, j, k);
+            for (int c = 0; c < 9; c++) go.g[c] = (R*)in.g[c];
+            go.dil = (R*)in.dil;
+            grad_point<R, V, sizeof(R) == 4>(I.g, I.cf, in.u, in.v, in.w, go, i, j, k);
         }
     }
     grid_barrier(bar, nb, err);
-    // phase 4: dilatation ghosts
+    // phase 3: dilatation ghosts
     for (long long u = blockIdx.x; u < ngu; u += gridDim.x) {
         const int q = find_inst(ctl->ghost_off, n, u);
         const BatchInst<R>& I = tab[q];
-        const long long t = (u - ctl->ghost_off[q]) * blockDim.x + threadIdx.x;
-        if (t < ghost_count(I.g)) ghost_scalar_cell<R>(I.g, I.dil, (int)t);
+        const long long t = (u - ctl->ghost_off[q]) * BATCH_THREADS + threadIdx.x;
+        if (t < ghost_count(I.g)) ghost_scalar_cell<R>(I.g, (R*)I.in[cur].dil, (int)t);
     }
     grid_barrier(bar, nb, err);
-    // phase 5: RHS + stage update into the other state buffer. The unit's x-y neighbourhood
-    // of the nine stencil fields is staged in shared memory, (32 + 2S) x (rows + 2S) per
-    // field, filled with coalesced row loads; z neighbours come from global memory. (Tile
-    // cells beyond the ghost layer, possible in the last unit of a row or column, are not
-    // read from memory; no thread uses them.)
-    constexpr int TX = 32 + 2 * S, FSMAX = TX * (8 + 2 * S);
-    __shared__ R tile[TF_COUNT * FSMAX];
-    const int FS = TX * (rows + 2 * S), nt = blockDim.x;
+    // phase 4: RHS + stage update into the other state buffer + that state's recovery, every
+    // neighbour from global memory (the standalone RHS kernel's point body)
     for (long long u = blockIdx.x; u < npu; u += gridDim.x) {
         const int q = find_inst(ctl->unit_off, n, u);
         const BatchInst<R>& I = tab[q];
-        const long long lu = u - ctl->unit_off[q];
-        const int bx = (int)(lu % I.nbx), by = (int)((lu / I.nbx) % I.nby), k = (int)(lu / ((long long)I.nbx * I.nby));
-        const int i0 = bx * 32, j0 = by * rows;
-        RhsIn<R> in;
-        if (I.s32[0]) { in.r = I.s32[0]; in.u = I.s32[1]; in.v = I.s32[2]; in.w = I.s32[3]; }
-        else {
-            in.r = (const R*)I.q[cur][0]; in.u = (const R*)I.q[cur][1];
-            in.v = (const R*)I.q[cur][2]; in.w = (const R*)I.q[cur][3];
-        }
-        in.h = I.der[0]; in.t = I.der[1]; in.p = I.der[2]; in.m = I.der[3]; in.dil = I.dil;
-        for (int c = 0; c < 9; c++) in.g[c] = I.grad[c];
-        __syncthreads();   // the previous unit is done with the tile
-        {
-            const long long org = I.g.at(i0 - S, j0 - S, k);
-            const int xlim = I.g.mx + 2 * S - i0, ylim = I.g.my + 2 * S - j0;
-            const long long P = I.g.P;
-            const R* src[TF_COUNT] = {in.u, in.v, in.w, in.r, in.h, in.p, in.t, in.m, in.dil};
-#pragma unroll
-            for (int f = 0; f < TF_COUNT; f++) {
-                for (int e = threadIdx.x; e < FS; e += nt) {
-                    const int yy = e / TX, xx = e - yy * TX;
-                    tile[f * FS + e] = (xx < xlim && yy < ylim) ? ld(src[f], (int)(org + (long long)yy * P + xx)) : (R)0;
-                }
-            }
-        }
-        __syncthreads();
-        const int i = i0 + tx, j = j0 + ty;
-        if (i < I.g.mx && j < I.g.my) {
-            Update<R> up;
-            up.kind = kind; up.a = a; up.b = b; up.ca = (R)a; up.cb = (R)b; up.use_prev = a != 0.0;
-            up.fuse = 0;   // this kernel recovers each stage's state in its own phase
-            up.qin = StateIn{I.q[cur][0], I.q[cur][1], I.q[cur][2], I.q[cur][3], I.q[cur][4]};
-            const int nx = 1 - cur;
-            up.qout = StateOut{I.q[nx][0], I.q[nx][1], I.q[nx][2], I.q[nx][3], I.q[nx][4]};
-            for (int c = 0; c < 5; c++) { up.rb[c] = I.rb[c]; up.k2[c] = nullptr; up.q0[c] = nullptr; }
-            up.spx = I.spx; up.spz = I.spz; up.rref = I.rref; up.uref = I.uref; up.vref = I.vref;
-            up.wref = I.wref; up.eref = I.eref;
-            const R* ctr = tile + (ty + S) * TX + (tx + S);
-            const NbTile<R> nbx{ctr, 1, FS}, nby{ctr, TX, FS};
-            const int c = (int)I.g.at(i, j, k);
-            const NbGlobal<R> nbz{&in, c, (int)I.g.PS};
-            rhs_point_nb<R, S, V>(I.g, I.cf, in, up, I.scal, quirk, i, k, c, nbx, nby, nbz, ctr[TF_DIL * FS],
-                                  ctr[TF_M * FS], ctr[TF_U * FS], ctr[TF_V * FS], ctr[TF_W * FS], ctr[TF_R * FS],
-                                  ctr[TF_H * FS]);
-        }
+        int i, j, k;
+        unit_point(I, u - ctl->unit_off[q], tx, ty, i, j, k);
+        if (i < I.g.mx && j < I.g.my)
+            rhs_point<R, S, V>(I.g, I.cf, I.in[cur], I.up[stage][cur], I.scal, quirk, i, j, k);
     }
 }
 

@@ -5,11 +5,11 @@
 namespace cns {
 
 template <typename R, int S, int V>
-cudaError_t batch_launch_t(dim3 grid, dim3 block, const BatchInst<R>* tab, const BatchCtl* ctl, int cur, int kind,
-                           double a, double b, int stage0, int quirk, unsigned* bar, int* err, cudaStream_t s) {
+cudaError_t batch_launch_t(dim3 grid, const BatchInst<R>* tab, const BatchCtl* ctl, int cur, int stage, int quirk,
+                           unsigned* bar, int* err, cudaStream_t s) {
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = grid;
-    cfg.blockDim = block;
+    cfg.blockDim = dim3(BATCH_THREADS);
     cfg.dynamicSmemBytes = 0;
     cfg.stream = s;
     cudaLaunchAttribute attr[1];
@@ -17,15 +17,14 @@ cudaError_t batch_launch_t(dim3 grid, dim3 block, const BatchInst<R>* tab, const
     attr[0].val.cooperative = 1;
     cfg.attrs = attr;
     cfg.numAttrs = 1;
-    return cudaLaunchKernelEx(&cfg, k_batch_stage<R, S, V>, tab, ctl, cur, kind, a, b, stage0, quirk, bar, err);
+    return cudaLaunchKernelEx(&cfg, k_batch_stage<R, S, V>, tab, ctl, cur, stage, quirk, bar, err);
 }
 
 template <typename R>
-cudaError_t batch_launch_dispatch(int S, int V, dim3 grid, dim3 block, const BatchInst<R>* tab, const BatchCtl* ctl,
-                                  int cur, int kind, double a, double b, int stage0, int quirk, unsigned* bar,
-                                  int* err, cudaStream_t s) {
+cudaError_t batch_launch_dispatch(int S, int V, dim3 grid, const BatchInst<R>* tab, const BatchCtl* ctl, int cur,
+                                  int stage, int quirk, unsigned* bar, int* err, cudaStream_t s) {
 #define CNS_BL(SS, VV) \
-    if (S == SS && V == VV) return batch_launch_t<R, SS, VV>(grid, block, tab, ctl, cur, kind, a, b, stage0, quirk, bar, err, s);
+    if (S == SS && V == VV) return batch_launch_t<R, SS, VV>(grid, tab, ctl, cur, stage, quirk, bar, err, s);
     CNS_BL(1, 1) CNS_BL(2, 1) CNS_BL(2, 2) CNS_BL(3, 1) CNS_BL(3, 2) CNS_BL(3, 3)
     CNS_BL(4, 1) CNS_BL(4, 2) CNS_BL(4, 3) CNS_BL(4, 4)
 #undef CNS_BL
@@ -33,9 +32,16 @@ cudaError_t batch_launch_dispatch(int S, int V, dim3 grid, dim3 block, const Bat
 }
 
 template <typename R>
-cudaError_t batch_occ_dispatch(int S, int V, int threads, int* nb) {
-#define CNS_BO(SS, VV) \
-    if (S == SS && V == VV) return cudaOccupancyMaxActiveBlocksPerMultiprocessor(nb, k_batch_stage<R, SS, VV>, threads, 0);
+cudaError_t batch_time_launch(const BatchInst<R>* tab, const BatchCtl* ctl, cudaStream_t s) {
+    k_batch_time<R><<<(CNS_BATCH_MAX + 127) / 128, 128, 0, s>>>(tab, ctl);
+    return cudaGetLastError();
+}
+
+template <typename R>
+cudaError_t batch_occ_dispatch(int S, int V, int* nb) {
+#define CNS_BO(SS, VV)   \
+    if (S == SS && V == VV) \
+        return cudaOccupancyMaxActiveBlocksPerMultiprocessor(nb, k_batch_stage<R, SS, VV>, BATCH_THREADS, 0);
     CNS_BO(1, 1) CNS_BO(2, 1) CNS_BO(2, 2) CNS_BO(3, 1) CNS_BO(3, 2) CNS_BO(3, 3)
     CNS_BO(4, 1) CNS_BO(4, 2) CNS_BO(4, 3) CNS_BO(4, 4)
 #undef CNS_BO

@@ -102,9 +102,8 @@ int check_params(const cns_params* p) {
 }
 
 template <typename R>
-RhsIn<R> rhs_in(cns_solver* h) {
+RhsIn<R> rhs_in(cns_solver* h, int c) {
     RhsIn<R> in;
-    const int c = h->cur;
     if (h->fp32) {
         in.r = (const R*)h->s32[c][0]; in.u = (const R*)h->s32[c][1]; in.v = (const R*)h->s32[c][2];
         in.w = (const R*)h->s32[c][3];
@@ -181,8 +180,10 @@ int grad_phase(cns_solver* h) {
     return CNS_OK;
 }
 
+// the stage update from state buffer c into 1 - c; with fuse, the RHS kernel also recovers
+// the new state's derived fields (the next stage's calcState)
 template <typename R>
-int rhs_phase(cns_solver* h, int kind, double a, double b) {
+Update<R> stage_update(cns_solver* h, int kind, double a, double b, int c, bool fuse) {
     Update<R> up{};
     up.kind = kind;
     up.a = a;
@@ -190,8 +191,8 @@ int rhs_phase(cns_solver* h, int kind, double a, double b) {
     up.ca = (R)a;
     up.cb = (R)b;
     up.use_prev = a != 0.0;
-    up.qin = state_in(h, h->cur);
-    const int nb = 1 - h->cur;
+    up.qin = state_in(h, c);
+    const int nb = 1 - c;
     up.qout = StateOut{h->q[nb][0], h->q[nb][1], h->q[nb][2], h->q[nb][3], h->q[nb][4]};
     for (int q = 0; q < 5; q++) {
         up.rb[q] = (R*)h->rb[q];
@@ -202,18 +203,25 @@ int rhs_phase(cns_solver* h, int kind, double a, double b) {
         up.spx = h->spx; up.spz = h->spz; up.rref = h->rref; up.uref = h->uref; up.vref = h->vref;
         up.wref = h->wref; up.eref = h->eref;
     }
-    if (kind != ST_RHS_ONLY) {   // the new state's recovery for the next stage
+    if (fuse) {
         up.fuse = 1;
         up.dnext = derived_out<R>(h, nb);
         up.ph = h->phys;
     }
+    return up;
+}
+
+template <typename R>
+int rhs_phase(cns_solver* h, int kind, double a, double b) {
+    const Update<R> up = stage_update<R>(h, kind, a, b, h->cur, kind != ST_RHS_ONLY);
+    const int nb = 1 - h->cur;
     const int quirk = h->p.quirk_dissipation_y != 0;
     if constexpr (std::is_same<R, float>::value)
-        launch_rhs_fp32(h->p.stencil_size, h->p.stencil_visc, h->geom, h->phys, h->cf32, rhs_in<float>(h), up, h->scal,
-                        quirk, h->stream);
+        launch_rhs_fp32(h->p.stencil_size, h->p.stencil_visc, h->geom, h->phys, h->cf32, rhs_in<float>(h, h->cur),
+                        up, h->scal, quirk, h->stream);
     else
-        launch_rhs_fp64(h->p.stencil_size, h->p.stencil_visc, h->geom, h->phys, h->cf64, rhs_in<double>(h), up,
-                        h->scal, quirk, h->stream);
+        launch_rhs_fp64(h->p.stencil_size, h->p.stencil_visc, h->geom, h->phys, h->cf64, rhs_in<double>(h, h->cur),
+                        up, h->scal, quirk, h->stream);
     h->launches += 1;
     CKL();
     if (kind != ST_RHS_ONLY) {
@@ -236,6 +244,20 @@ int rhs_any(cns_solver* h, int kind, double a, double b) {
 }
 
 }  // namespace
+
+namespace cns {
+template <typename R>
+RhsIn<R> solver_rhs_in(cns_solver* h, int b) { return rhs_in<R>(h, b); }
+template <typename R>
+Update<R> solver_stage_update(cns_solver* h, int kind, double a, double b, int c) {
+    return stage_update<R>(h, kind, a, b, c, true);
+}
+template RhsIn<float> solver_rhs_in<float>(cns_solver*, int);
+template RhsIn<double> solver_rhs_in<double>(cns_solver*, int);
+template Update<float> solver_stage_update<float>(cns_solver*, int, double, double, int);
+template Update<double> solver_stage_update<double>(cns_solver*, int, double, double, int);
+int solver_ensure_state(cns_solver* h) { return ensure_state(h); }
+}  // namespace cns
 
 int cns::solver_reduce(cns_solver* h, int want, double* diag) {
     if (h->fp32) launch_reduce<float>(h->geom, h->phys, state_in(h, h->cur), (const float*)h->der[h->mu_buf][3], h->part, want,

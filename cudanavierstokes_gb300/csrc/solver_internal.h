@@ -129,6 +129,15 @@ inline void solver_set_parity(cns_solver* h, int want) {
     h->drop_graphs();
 }
 int solver_reduce(cns_solver* h, int want, double* diag);
+// stencil inputs (+ theta, gradients) of state buffer b
+template <typename R>
+RhsIn<R> solver_rhs_in(cns_solver* h, int b);
+// stage update of the given kind from state buffer c into 1 - c, with the fused recovery of
+// the new state's derived fields
+template <typename R>
+Update<R> solver_stage_update(cns_solver* h, int kind, double a, double b, int c);
+// recover the current state's derived fields unless they are current
+int solver_ensure_state(cns_solver* h);
 // one time step of the handle's scheme on h->stream (through its step graph when graphs
 // are on), logging the time at the device step counter up to diag_cap entries
 int solver_step(cns_solver* h);

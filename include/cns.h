@@ -280,8 +280,8 @@ CNS_API int cns_batch_member_steps(cns_batch* b, int id, int64_t* steps);
 CNS_API int cns_batch_info(cns_batch* b, int* count, int64_t* points, int64_t* bytes, int64_t* launches);
 /* Advance every member by nsteps steps. */
 CNS_API int cns_batch_step(cns_batch* b, int nsteps);
-/* Launch shape of the persistent stage kernel: 128 or 256 threads per block, blocks per SM
- * (clamped to the co-residency limit). */
+/* Launch shape of the persistent stage kernel: 128 threads per block (the only shape; a work
+ * unit is a 32 x 4 tile of an x-y plane), blocks per SM (clamped to the co-residency limit). */
 CNS_API int cns_batch_set_shape(cns_batch* b, int threads, int blocks_per_sm);
 CNS_API int cns_batch_get_shape(cns_batch* b, int* threads, int* blocks_per_sm);
 
