@@ -20,7 +20,11 @@ reference itself. Steps:
           gpurun_out/ref_golden/<case>.npz.
   collect (back in the container) copy the packed results to tests/golden/.
 
-Usage: python oracle/ref_harness.py {stage|run|collect} [case ...]
+  time    (on the GPU machine) build and run the staged timing cases (the benchmark channel
+          at two run lengths) and write the reference's per-step time to
+          gpurun_out/ref_timing.json.
+
+Usage: python oracle/ref_harness.py {stage|run|time|collect} [case ...]
 """
 from __future__ import annotations
 
@@ -68,6 +72,17 @@ def cases():
         # boundary layer: extrapolated x top / z ends, sponge, wall perturbation
         "bl_16x8x160_s3v2": dict(params=boundary_layer_params(16, 8, 160), nsteps=6, ic="bl"),
     }
+
+
+def timing_cases():
+    """Throughput of the reference's own GPU code on the benchmark channel (reference axes
+    mx=128 wall-normal, my=160 span, mz=192 stream; S = V = 4, Wray RK3, FP64), started
+    from the reference's own channel initialisation (restartFile = -1). Two runs of
+    different length: the per-step time is their difference quotient, which cancels the
+    set-up, the initial-field generation and the file output inside the reference's own
+    total time (src/main.cpp:71-75)."""
+    p = channel_params(128, 160, 192)
+    return {f"time_channel_128x160x192_n{n}": dict(params=p, nsteps=n, ic="ref_init") for n in (20, 80)}
 
 
 def _lit(x: float) -> str:
@@ -197,8 +212,8 @@ def blasius_like_profile(n: int = 601, xmax: float = 60.0):
 def stage(names):
     if not os.path.isdir(REF_SRC):
         raise SystemExit(f"reference sources not found at {REF_SRC}")
-    allc = cases()
-    for name in names or allc:
+    allc = dict(cases(), **timing_cases())
+    for name in names or cases():
         c = allc[name]
         p, nsteps = c["params"], c["nsteps"]
         d = os.path.join(STAGE_ROOT, name)
@@ -215,12 +230,14 @@ def stage(names):
         with open(cm, "w") as f:
             f.write(_disable_dead_helpers(txt))
         shutil.copy(os.path.join(HERE, "ref_mpi_stub.h"), os.path.join(d, "src", "mpi.h"))
-        restart = -1 if c["ic"] == "bl" else 0
+        restart = -1 if c["ic"] in ("bl", "ref_init") else 0
         with open(os.path.join(d, "src", "globals.h"), "w") as f:
             f.write(parameter_header(p, nsteps, restart))
         with open(os.path.join(d, "Makefile"), "w") as f:
             f.write(MAKEFILE)
-        if c["ic"] == "bl":
+        if c["ic"] == "ref_init":
+            pass
+        elif c["ic"] == "bl":
             os.makedirs(os.path.join(d, "blasius1D"))
             for nm, arr in zip("xruwe", blasius_like_profile()):
                 arr.astype(np.float64).tofile(os.path.join(d, "blasius1D", f"{nm}Prof.bin"))
@@ -240,7 +257,7 @@ def stage(names):
 
 def run(names):
     os.makedirs(OUT_ROOT, exist_ok=True)
-    dirs = sorted(n for n in os.listdir(STAGE_ROOT) if os.path.isdir(os.path.join(STAGE_ROOT, n)))
+    dirs = sorted(n for n in os.listdir(STAGE_ROOT) if os.path.isdir(os.path.join(STAGE_ROOT, n)) and n in cases())
     ok = True
     for name in dirs:
         if names and name not in names:
@@ -286,6 +303,53 @@ def run(names):
     return ok
 
 
+def time_runs(names):
+    """Build and run the staged timing cases twice each: in the reference's native stream
+    order (its default, unsynchronised) and with CUDA_LAUNCH_BLOCKING=1 (program order),
+    and write the per-step times and Mpoint-steps/s to gpurun_out/ref_timing.json."""
+    tc = timing_cases()
+    os.makedirs(OUT_ROOT, exist_ok=True)
+    res = {}
+    for name in sorted(tc):
+        if names and name not in names:
+            continue
+        d = os.path.join(STAGE_ROOT, name)
+        shutil.rmtree(os.path.join(d, "obj"), ignore_errors=True)
+        if os.path.exists(os.path.join(d, "ns")):
+            os.remove(os.path.join(d, "ns"))
+        b = subprocess.run(["make", "-j", str(os.cpu_count() or 4)], cwd=d, capture_output=True, text=True)
+        if b.returncode != 0:
+            print(f"[{name}] build failed:\n{b.stderr[-3000:]}")
+            return False
+        for mode, extra in (("native", {}), ("blocking", {"CUDA_LAUNCH_BLOCKING": "1"})):
+            r = subprocess.run(["./ns"], cwd=d, capture_output=True, text=True, env=dict(os.environ, **extra),
+                               timeout=900)
+            log = r.stdout + r.stderr
+            with open(os.path.join(OUT_ROOT, f"{name}_{mode}.log"), "w") as f:
+                f.write(log)
+            m = re.search(r"The total time is:\s+(\S+)", log)
+            if r.returncode != 0 or not m:
+                print(f"[{name}/{mode}] run failed rc={r.returncode}\n{log[-2000:]}")
+                return False
+            steps = re.findall(r"step number (\d+) with (\S+) (\S+)", log)
+            res[f"{name}/{mode}"] = dict(total_s=float(m.group(1)), nsteps=tc[name]["nsteps"],
+                                         last_dt=float(steps[-1][1]) if steps else None)
+            print(f"[{name}/{mode}] total {float(m.group(1)):.3f} s")
+    out = {"runs": res}
+    p = timing_cases()[sorted(tc)[0]]["params"]
+    pts = p.mx * p.my * p.mz
+    for mode in ("native", "blocking"):
+        a, b = (res.get(f"{n}/{mode}") for n in sorted(tc, key=lambda n: tc[n]["nsteps"]))
+        if a and b:
+            per = (b["total_s"] - a["total_s"]) / (b["nsteps"] - a["nsteps"])
+            out[mode] = dict(s_per_step=per, mpoint_steps_per_s=pts / per / 1e6)
+    os.makedirs(OUT_ROOT, exist_ok=True)
+    with open(os.path.join(OUT_ROOT, "ref_timing.json"), "w") as f:
+        json.dump(out, f, indent=1)
+    print(json.dumps(out))
+    return True
+
+
 def collect(names):
     os.makedirs(GOLDEN, exist_ok=True)
     for fn in sorted(os.listdir(OUT_ROOT)):
@@ -301,6 +365,8 @@ if __name__ == "__main__":
         stage(names)
     elif cmd == "run":
         sys.exit(0 if run(names) else 1)
+    elif cmd == "time":
+        sys.exit(0 if time_runs(names) else 1)
     elif cmd == "collect":
         collect(names)
     else:
