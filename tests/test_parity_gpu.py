@@ -201,10 +201,9 @@ def test_fp32_rhs_channel(gpu_lib, oracle_mod):
     assert max(errs) <= 1e-4, errs
 
 
-def test_fp32_rhs_plane_marching_kernel(gpu_lib, oracle_mod):
-    """A grid large enough for the FP32 RHS kernel that streams z planes through shared
-    memory by TMA (stretched channel with walls), against the FP64 oracle: one RHS and
-    five steps."""
+def test_fp32_rhs_larger_channel(gpu_lib, oracle_mod):
+    """A larger stretched channel with walls (many blocks per plane) against the FP64
+    oracle: one RHS and five steps."""
     p = channel_params(64, 64, 48)
     o = oracle_mod.Oracle(p)
     f = wall_state(p, o.grid()["x"])
@@ -215,6 +214,36 @@ def test_fp32_rhs_plane_marching_kernel(gpu_lib, oracle_mod):
     assert max(errs) <= 1e-4, errs
     o.run(5)
     s.run(5)
+    assert max(state_errors(s.copy_field_out(), o.get_state())) <= 2e-6
+
+
+@pytest.mark.parametrize("S,V", SV)
+def test_fp32_rhs_all_orders_odd_edges(gpu_lib, oracle_mod, S, V):
+    """The FP32 RHS at every stencil order on a periodic box with odd, unequal edges (a
+    partial last block in x and y) against the FP64 oracle."""
+    p = tgv_params(17).copy(my=12, mz=10, stencil_size=S, stencil_visc=V)
+    f = smooth_random_state(p, seed=S * 10 + V)
+    o = oracle_mod.Oracle(p)
+    o.set_state(*f)
+    s = Solver(p.copy(precision=PREC_FP32_RHS))
+    s.copy_field_in(*f)
+    errs = field_errors(s.calc_rhs(), o.rhs())
+    assert max(errs) <= 2e-5, errs
+
+
+def test_fp32_channel_odd_mx(gpu_lib, oracle_mod):
+    """Stretched channel with walls and an odd wall-normal size (non-uniform x tables):
+    RHS and three steps against the FP64 oracle."""
+    p = channel_params(25, 16, 20)
+    o = oracle_mod.Oracle(p)
+    f = wall_state(p, o.grid()["x"])
+    o.set_state(*f)
+    s = Solver(p.copy(precision=PREC_FP32_RHS))
+    s.copy_field_in(*f)
+    errs = field_errors(s.calc_rhs(), o.rhs())
+    assert max(errs) <= 1e-4, errs
+    o.run(3)
+    s.run(3)
     assert max(state_errors(s.copy_field_out(), o.get_state())) <= 2e-6
 
 
