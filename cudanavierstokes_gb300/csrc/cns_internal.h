@@ -86,7 +86,7 @@ template <typename R>
 void launch_ghost_scalar(const Geom& g, R* f, cudaStream_t s);
 template <typename R>
 void launch_grad(int V, const Geom& g, const CoefT<R>& cf, const R* u, const R* v, const R* w, const GradOut<R>& o,
-                 cudaStream_t s);
+                 int own, cudaStream_t s);
 template <typename R>
 int launch_reduce(const Geom& g, const Phys& ph, const StateIn& q, const R* mu, double* part, int want, double* scal,
                   double* diag, cudaStream_t s);

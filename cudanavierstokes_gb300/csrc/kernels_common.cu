@@ -31,11 +31,11 @@ __global__ void __launch_bounds__(256) k_ghost_state(Geom g, Phys ph, StencilFie
 
 template <typename R, int V>
 __global__ void __launch_bounds__(128) k_grad(Geom g, CoefT<R> cf, const R* __restrict__ u, const R* __restrict__ v,
-                                              const R* __restrict__ w, GradOut<R> o) {
+                                              const R* __restrict__ w, GradOut<R> o, int own) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     const int j = blockIdx.y * blockDim.y + threadIdx.y;
     if (i >= g.mx || j >= g.my) return;
-    grad_point<R, V, sizeof(R) == 4>(g, cf, u, v, w, o, i, j, (int)blockIdx.z);
+    grad_point<R, V, sizeof(R) == 4>(g, cf, u, v, w, o, i, j, (int)blockIdx.z, own != 0);
 }
 
 template <typename R>
@@ -200,12 +200,12 @@ void launch_ghost_scalar(const Geom& g, R* f, cudaStream_t s) {
 }
 template <typename R>
 void launch_grad(int V, const Geom& g, const CoefT<R>& cf, const R* u, const R* v, const R* w, const GradOut<R>& o,
-                 cudaStream_t s) {
+                 int own, cudaStream_t s) {
     switch (V) {
-    case 1: k_grad<R, 1><<<point_grid(g), point_block(), 0, s>>>(g, cf, u, v, w, o); break;
-    case 2: k_grad<R, 2><<<point_grid(g), point_block(), 0, s>>>(g, cf, u, v, w, o); break;
-    case 3: k_grad<R, 3><<<point_grid(g), point_block(), 0, s>>>(g, cf, u, v, w, o); break;
-    default: k_grad<R, 4><<<point_grid(g), point_block(), 0, s>>>(g, cf, u, v, w, o); break;
+    case 1: k_grad<R, 1><<<point_grid(g), point_block(), 0, s>>>(g, cf, u, v, w, o, own); break;
+    case 2: k_grad<R, 2><<<point_grid(g), point_block(), 0, s>>>(g, cf, u, v, w, o, own); break;
+    case 3: k_grad<R, 3><<<point_grid(g), point_block(), 0, s>>>(g, cf, u, v, w, o, own); break;
+    default: k_grad<R, 4><<<point_grid(g), point_block(), 0, s>>>(g, cf, u, v, w, o, own); break;
     }
 }
 template <typename R>
@@ -234,7 +234,7 @@ void launch_pack(const Geom& g, const T* src, double* dst, cudaStream_t s) {
                                         cudaStream_t);                                                           \
     template void launch_ghost_scalar<R>(const Geom&, R*, cudaStream_t);                                          \
     template void launch_grad<R>(int, const Geom&, const CoefT<R>&, const R*, const R*, const R*, const GradOut<R>&,  \
-                                 cudaStream_t);                                                                  \
+                                 int, cudaStream_t);                                                             \
     template int launch_reduce<R>(const Geom&, const Phys&, const StateIn&, const R*, double*, int, double*,      \
                                   double*, cudaStream_t);                                                        \
     template void launch_unpack<R>(const Geom&, const double*, R*, cudaStream_t);                                 \

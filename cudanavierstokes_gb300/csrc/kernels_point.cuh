@@ -190,10 +190,33 @@ __device__ __forceinline__ void ghost_state_cell(const Geom& g, const Phys& ph, 
 // ---------------------------------------------------------------------------------
 // DIL_ONLY: only the three diagonal gradients and theta (the FP32-RHS kernel forms the nine
 // gradients itself from the velocity stencils it loads, and needs theta at its neighbours)
+// Ghost images of the dilatation at interior point (i, j, k), element c, written by the point
+// itself where every dilatation ghost is a copy of one interior value (x periodic or wall:
+// even mirror; y, z periodic), which makes the dilatation ghost fill unnecessary
+template <typename R>
+__device__ __forceinline__ void dil_ghost_owner(const Geom& g, R* __restrict__ f, long long c, int i, int j, int k,
+                                                R val) {
+    const int G = g.G;
+    if (g.xbc == XBC_PER) {
+        if (i < G) f[c + g.mx] = val;
+        if (i >= g.mx - G) f[c - g.mx] = val;
+    } else {   // wall: the ghost at -1 - i (bottom) or 2 mx - 1 - i (top) mirrors i
+        if (i < G) f[c - 1 - 2 * i] = val;
+        if (i >= g.mx - G) f[c + 2 * (g.mx - i) - 1] = val;
+    }
+    const long long ly = (long long)g.my * g.P, lz = (long long)g.mz * g.PS;
+    if (j < G) f[c + ly] = val;
+    if (j >= g.my - G) f[c - ly] = val;
+    if (k < G) f[c + lz] = val;
+    if (k >= g.mz - G) f[c - lz] = val;
+}
+
+// own: also write the dilatation's ghost images (dil_ghost_owner; periodic and wall x,
+// periodic z only)
 template <typename R, int V, bool DIL_ONLY = false>
 __device__ __forceinline__ void grad_point(const Geom& g, const CoefT<R>& cf, const R* __restrict__ u,
                                            const R* __restrict__ v, const R* __restrict__ w, const GradOut<R>& o,
-                                           int i, int j, int k) {
+                                           int i, int j, int k, bool own = false) {
     const long long c = g.at(i, j, k);
     const long long st[3] = {1, g.P, g.PS};
     const R* F[3] = {u, v, w};
@@ -216,7 +239,9 @@ __device__ __forceinline__ void grad_point(const Geom& g, const CoefT<R>& cf, co
 #pragma unroll
         for (int q = 0; q < 9; q++) o.g[q][c] = out[q];
     }
-    o.dil[c] = out[0] + out[4] + out[8];
+    const R th = out[0] + out[4] + out[8];
+    o.dil[c] = th;
+    if (own) dil_ghost_owner<R>(g, o.dil, c, i, j, k, th);
 }
 
 // Dilatation ghost cell t (BCxNumber2 / BCyNumber1 / BCzNumber1): x periodic | wall:

@@ -173,9 +173,15 @@ int grad_phase(cns_solver* h) {
     const CoefT<R>* cfp;
     if constexpr (std::is_same<R, float>::value) cfp = &h->cf32; else cfp = &h->cf64;
     const CoefT<R>& cf = *cfp;
-    launch_grad<R>(h->p.stencil_visc, h->geom, cf, u, v, w, o, h->stream);
-    launch_ghost_scalar<R>(h->geom, (R*)h->dil, h->stream);
-    h->launches += 2;
+    // every dilatation ghost is a copy of one interior value unless the boundary layer
+    // extrapolates: then the gradient kernel writes them itself
+    const bool own = h->geom.xbc != XBC_BL && !h->geom.zbl;
+    launch_grad<R>(h->p.stencil_visc, h->geom, cf, u, v, w, o, own ? 1 : 0, h->stream);
+    h->launches += 1;
+    if (!own) {
+        launch_ghost_scalar<R>(h->geom, (R*)h->dil, h->stream);
+        h->launches += 1;
+    }
     CKL();
     return CNS_OK;
 }
