@@ -26,10 +26,8 @@ namespace cns {
 template <typename R>
 __device__ __forceinline__ R ld(const R* __restrict__ p, int o) { return __ldg(p + o); }
 
-// Neighbours of the centre point along one direction: in global memory at a stride, or in
-// a shared-memory plane tile (the persistent batch kernel; fields in the tile order TF_*).
-enum { TF_U, TF_V, TF_W, TF_R, TF_H, TF_P, TF_T, TF_M, TF_DIL, TF_COUNT };
-
+// Neighbours of the centre point along one direction, in global memory at a stride.
+//
 // Element offsets are 32-bit: every padded field holds fewer than 2^31 elements (checked
 // when a solver is created), and 64-bit offset arithmetic costs two integer instructions
 // per neighbour address.
@@ -46,22 +44,6 @@ struct NbGlobal {
     __device__ __forceinline__ R t(int l) const { return ld(in->t, c + l * st); }
     __device__ __forceinline__ R m(int l) const { return ld(in->m, c + l * st); }
     __device__ __forceinline__ R dil(int l) const { return ld(in->dil, c + l * st); }
-};
-
-template <typename R>
-struct NbTile {
-    const R* ctr;   // the centre point in field 0 of the tile
-    int step, fs;   // neighbour step (1 along x, the tile width along y), field stride
-    __device__ __forceinline__ R at(int f, int l) const { return ctr[f * fs + l * step]; }
-    __device__ __forceinline__ R u(int l) const { return at(TF_U, l); }
-    __device__ __forceinline__ R v(int l) const { return at(TF_V, l); }
-    __device__ __forceinline__ R w(int l) const { return at(TF_W, l); }
-    __device__ __forceinline__ R r(int l) const { return at(TF_R, l); }
-    __device__ __forceinline__ R h(int l) const { return at(TF_H, l); }
-    __device__ __forceinline__ R p(int l) const { return at(TF_P, l); }
-    __device__ __forceinline__ R t(int l) const { return at(TF_T, l); }
-    __device__ __forceinline__ R m(int l) const { return at(TF_M, l); }
-    __device__ __forceinline__ R dil(int l) const { return at(TF_DIL, l); }
 };
 
 // first derivative sum_k co[k] (f_k - f_-k) and second derivative co[0] f_0 +
