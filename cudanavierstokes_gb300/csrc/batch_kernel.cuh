@@ -81,6 +81,38 @@ __device__ __forceinline__ int find_inst(const long long* off, int n, long long 
     return lo;
 }
 
+// One instance's parameters of the RHS phase for one stage and parity
+template <typename R>
+struct StageParams {
+    Geom g;
+    CoefT<R> cf;
+    RhsIn<R> in;
+    Update<R> up;
+    double* scal;
+    int nbx, nby;
+};
+
+// block-cooperative copy of an instance's stage parameters into shared memory (whole words)
+template <typename R>
+__device__ __forceinline__ void stage_params_copy(StageParams<R>& sp, const BatchInst<R>& I, int cur, int stage) {
+    const auto copy = [&](void* dst, const void* src, int bytes) {
+        for (int w = threadIdx.x; w < bytes / 4; w += blockDim.x)
+            static_cast<unsigned*>(dst)[w] = static_cast<const unsigned*>(src)[w];
+    };
+    static_assert(sizeof(Geom) % 4 == 0 && sizeof(CoefT<R>) % 4 == 0 && sizeof(RhsIn<R>) % 4 == 0 &&
+                      sizeof(Update<R>) % 4 == 0,
+                  "word copies");
+    copy(&sp.g, &I.g, sizeof(Geom));
+    copy(&sp.cf, &I.cf, sizeof(CoefT<R>));
+    copy(&sp.in, &I.in[cur], sizeof(RhsIn<R>));
+    copy(&sp.up, &I.up[stage][cur], sizeof(Update<R>));
+    if (threadIdx.x == 0) {
+        sp.scal = I.scal;
+        sp.nbx = I.nbx;
+        sp.nby = I.nby;
+    }
+}
+
 // Stage 0 of a step: every instance's time advances by its dt (before the ghost fill,
 // which reads the time in the boundary-layer wall perturbation)
 template <typename R>
@@ -152,14 +184,31 @@ __global__ void __launch_bounds__(BATCH_THREADS, sizeof(R) == 4 ? 5 : 4)
     }
     grid_barrier(bar, nb, err);
     // phase 4: RHS + stage update into the other state buffer + that state's recovery, every
-    // neighbour from global memory (the standalone RHS kernel's point body)
+    // neighbour from global memory (the standalone RHS kernel's point body). The unit's
+    // instance parameters (geometry, coefficients, inputs, stage update) are staged in
+    // shared memory when the instance changes: the point body reads them there instead of
+    // through the table in global memory.
+    __shared__ StageParams<R> sp;
+    int qs = -1;
     for (long long u = blockIdx.x; u < npu; u += gridDim.x) {
         const int q = find_inst(ctl->unit_off, n, u);
-        const BatchInst<R>& I = tab[q];
+        if (q != qs) {
+            __syncthreads();   // the previous unit is done with sp
+            stage_params_copy<R>(sp, tab[q], cur, stage);
+            __syncthreads();
+            qs = q;
+        }
         int i, j, k;
-        unit_point(I, u - ctl->unit_off[q], tx, ty, i, j, k);
-        if (i < I.g.mx && j < I.g.my)
-            rhs_point<R, S, V>(I.g, I.cf, I.in[cur], I.up[stage][cur], I.scal, quirk, i, j, k);
+        const long long lu = u - ctl->unit_off[q];
+        {
+            const long long pl = (long long)sp.nbx * sp.nby;
+            k = (int)(lu / pl);
+            const int r = (int)(lu - (long long)k * pl);
+            const int by = r / sp.nbx, bx = r - by * sp.nbx;
+            i = bx * 32 + tx;
+            j = by * 4 + ty;
+        }
+        if (i < sp.g.mx && j < sp.g.my) rhs_point<R, S, V>(sp.g, sp.cf, sp.in, sp.up, sp.scal, quirk, i, j, k);
     }
 }
 
