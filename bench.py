@@ -54,7 +54,11 @@ def parse_args():
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
-    ap.add_argument("--workload", choices=["channel", "tgv", "precision"], default="channel")
+    ap.add_argument("--workload", choices=["channel", "tgv", "precision", "batch"], default="channel")
+    ap.add_argument("--batch-members", type=int, default=48,
+                    help="batch workload: the first N members of the 48-member ensemble")
+    ap.add_argument("--batch-mode", choices=["tuned", "persistent", "concurrent"], default="tuned",
+                    help="batch workload: execution mode (tuned: the autotuner's pick)")
     ap.add_argument("--t-end", type=float, default=10.0, help="precision study: end time")
     ap.add_argument("--precision", choices=["fp64", "fp32"], default="fp64")
     ap.add_argument("--no-extras", action="store_true", help="skip fp32/cpu/e2e side measurements")
@@ -193,19 +197,25 @@ def cpu_sample(p, steps_min: int = 2, seconds: float = 12.0):
                                                     f"({pts} points, same physics and stencils), {dt:.1f} s")
 
 
-def run_batched(args, stream_ptr):
-    """BASELINE config 3: the 48-member ensemble in FP32-RHS mode, in the execution mode and
-    launch shape the autotuner picks; the other mode is timed beside it for the record."""
+def run_batched(args, stream_ptr, members=48, mode_req="tuned", with_other=True):
+    """BASELINE config 3: the 48-member ensemble (or its first `members`) in FP32-RHS mode,
+    in the execution mode and launch shape the autotuner picks (or the mode requested, at
+    full residency); the other mode is timed beside it for the record."""
     import torch
     from cudanavierstokes_gb300.batch import Batch
     from cudanavierstokes_gb300.workloads import ensemble, ensemble_fields
-    mem = ensemble(48, seed=0)
+    mem = ensemble(48, seed=0)[:members]
     bt = Batch(precision=1)
     bt.set_stream(stream_ptr)
     total_steps = 2 * args.warmup + 2 * args.steps + 128
     for p, ph in mem:
         bt.add(p, ensemble_fields(p, ph), max_steps=total_steps)
-    tuned_ms = bt.tune(2)
+    tuned_ms = None
+    if mode_req == "tuned":
+        tuned_ms = bt.tune(2)
+    else:
+        bt.set_mode(0 if mode_req == "persistent" else 1)
+        bt.set_shape(128, 32)   # full residency: clamped to the kernel's co-residency limit
     stream = torch.cuda.ExternalStream(stream_ptr)
 
     def timed():
@@ -230,6 +240,9 @@ def run_batched(args, stream_ptr):
            "tune_ms_per_step": tuned_ms, "kernel_launches_timed": launches,
            "workload": "48 Taylor-Green boxes, edge in {32,48,64,96,128}, Re log-U[400,3200], Ma U[0.1,0.8], "
                        "seeded phases (seed 0), 8th order, Wray RK3, FP32 RHS / FP64 state"}
+    if not with_other:
+        bt.close()
+        return out
     # the other execution mode on the same members
     other = 1 - mode
     bt.set_mode(other)
@@ -513,12 +526,30 @@ def run_gb300(args, world, rank, local):
         print(json.dumps(line), flush=True)
 
 
+def run_batch_only(args):
+    """The batched ensemble alone (for profiling the batch kernels): one JSON line."""
+    import torch
+    from cudanavierstokes_gb300.batch import Batch  # noqa: F401  (loads the library)
+    torch.cuda.init()
+    stream = torch.cuda.Stream()
+    res = run_batched(args, stream.cuda_stream, members=args.batch_members, mode_req=args.batch_mode,
+                      with_other=False)
+    print(json.dumps({"metric": "Mpoint-steps/s", "value": res["value"], "unit": "Mpoint-steps/s", "n_gpus": 1,
+                      "steps": args.steps, "warmup": args.warmup, "ms_per_step": res["ms_per_step"],
+                      "higher_is_better": True, "dtype": "f32-rhs/f64-state", "data": "synthetic",
+                      "config": {"workload": res["workload"], "members": res["members"], "points": res["points"],
+                                 "mode": res["mode"], "launch_shape": res["launch_shape"]}}))
+
+
 def main():
     args = parse_args()
     world, rank, local = dist_setup()
     if args.workload == "precision":
         if rank == 0:
             run_precision(args)
+    elif args.workload == "batch":
+        if rank == 0:
+            run_batch_only(args)
     elif args.impl == "reference":
         run_reference(args, world, rank)
     else:
