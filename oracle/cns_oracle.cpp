@@ -4,13 +4,13 @@
  * CPU restatement of the CudaNavierStokes time-advance path (state recovery,
  * velocity gradients, dilatation, split-form RHS in x/y/z with boundary conditions,
  * sponge, body force, CFL dt, bulk diagnostics, Wray low-storage RK3 and classic RK3).
- * It is the parity checker for the GPU library and the timed CPU baseline. It follows
+ * It is the parity reference for the GPU library and the timed CPU baseline. It follows
  * the reference kernels line by line, including their arithmetic order, the
  * double-interface flux loops and the y viscous-dissipation quirk, and processes
  * padded lines exactly as the reference's shared-memory pencils do.
  *
  * Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg may load this
- * library, and only as the checker / baseline. The product (cudanavierstokes_gb300)
+ * library, and only as the test oracle / CPU baseline. The product (cudanavierstokes_gb300)
  * never links or calls it.
  *
  * Reference files followed (paths inside the CudaNavierStokes project):

@@ -1,7 +1,7 @@
 """TEST INFRASTRUCTURE ONLY: ctypes wrapper of the CPU oracle (oracle/cns_oracle.cpp).
 
 The oracle is a CPU restatement of the CudaNavierStokes time-advance path used as the
-parity checker and as the timed CPU baseline. Only tests/, __graft_entry__.smoke() and
+parity reference and as the timed CPU baseline. Only tests/, __graft_entry__.smoke() and
 bench.py's CPU-baseline leg may import this module; the product never does.
 """
 from __future__ import annotations

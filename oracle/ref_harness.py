@@ -4,7 +4,7 @@ produce golden vectors that pin the CPU oracle (and, through it, the GB300 libra
 The reference has no CPU path and no tests, so parity is pinned by running the
 reference itself. Steps:
 
-  stage   (in the container that has the reference checkout)
+  stage   (on a machine with the reference checkout)
           For every case below: copy the reference's src/ into oracle/_ref/<case>/src
           (git-ignored, never committed), write a generated parameter header in place of
           its compile-time src/globals.h, add oracle/ref_mpi_stub.h as mpi.h, wrap the
@@ -12,17 +12,18 @@ reference itself. Steps:
           which CUDA >= 12 rejects) in `#if 0`, write the initial fields as restart
           files fields/*.0000000.bin (or, for the boundary layer, synthetic self-similar
           profiles blasius1D/*.bin) and a Makefile.
-  run     (on the GPU machine) `make` each case for sm_103a and run ./ns with
+  run     (on a GB300 host) `make` each case for sm_103a and run ./ns with
           CUDA_LAUNCH_BLOCKING=1 (program order: the reference's streams race otherwise),
           then pack initial and final fields, the dt/dpdz log, the friction Reynolds
           number the reference prints for the initial field (printRes) and its prof.txt
           plane profiles of the final field (calcAvgChan) into
-          gpurun_out/ref_golden/<case>.npz.
-  collect (back in the container) copy the packed results to tests/golden/.
+          <OUT_ROOT>/<case>.npz.
+  collect (back on the machine with the checkout) copy the packed results to
+          tests/golden/.
 
-  time    (on the GPU machine) build and run the staged timing cases (the benchmark channel
-          at two run lengths) and write the reference's per-step time to
-          gpurun_out/ref_timing.json.
+  time    (on a GB300 host) build and run the staged timing cases (the benchmark
+          channel at two run lengths) and write the reference's per-step time to
+          <OUT_ROOT>/ref_timing.json.
 
 Usage: python oracle/ref_harness.py {stage|run|time|collect} [case ...]
 """
@@ -48,6 +49,7 @@ from cudanavierstokes_gb300 import initial  # noqa: E402
 
 REF_SRC = "/root/reference/src"
 STAGE_ROOT = os.path.join(HERE, "_ref")
+# results of the runs on the GB300 host, in the folder whose contents come back from it
 OUT_ROOT = os.path.join(REPO, "gpurun_out", "ref_golden")
 GOLDEN = os.path.join(REPO, "tests", "golden")
 
@@ -306,7 +308,7 @@ def run(names):
 def time_runs(names):
     """Build and run the staged timing cases twice each: in the reference's native stream
     order (its default, unsynchronised) and with CUDA_LAUNCH_BLOCKING=1 (program order),
-    and write the per-step times and Mpoint-steps/s to gpurun_out/ref_timing.json."""
+    and write the per-step times and Mpoint-steps/s to <OUT_ROOT>/ref_timing.json."""
     tc = timing_cases()
     os.makedirs(OUT_ROOT, exist_ok=True)
     res = {}

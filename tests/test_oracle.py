@@ -1,4 +1,4 @@
-"""CPU tests of the oracle (the CPU restatement used as checker and CPU baseline):
+"""CPU tests of the oracle (the CPU restatement used as the parity reference and CPU baseline):
 grid, stencil order, conservation, dt formula, time order, boundary images."""
 import math
 
