@@ -184,12 +184,6 @@ __device__ __forceinline__ void ghost_state_cell(const Geom& g, const Phys& ph, 
     for (int q = 0; q < 8; q++) F[q][cg] = v[q];
 }
 
-// ---------------------------------------------------------------------------------
-// Velocity gradients gij[0..8] = d(u,v,w)/d(x,y,z) at the viscous order and the
-// dilatation (derVelX/Y/Z + calcDil, src/calc_stress.cu:20-63,87-96).
-// ---------------------------------------------------------------------------------
-// DIL_ONLY: only the three diagonal gradients and theta (the FP32-RHS kernel forms the nine
-// gradients itself from the velocity stencils it loads, and needs theta at its neighbours)
 // Ghost images of the dilatation at interior point (i, j, k), element c, written by the point
 // itself where every dilatation ghost is a copy of one interior value (x periodic or wall:
 // even mirror; y, z periodic), which makes the dilatation ghost fill unnecessary
@@ -211,8 +205,67 @@ __device__ __forceinline__ void dil_ghost_owner(const Geom& g, R* __restrict__ f
     if (k >= g.mz - G) f[c - lz] = val;
 }
 
+// Ghost cell t of the velocity alone (the u, v, w part of ghost_state_cell, for FP64
+// velocity fields whose other stencil inputs are not needed: the dissipation diagnostic)
+__device__ __forceinline__ void ghost_vel_cell(const Geom& g, const Phys& ph, double* u, double* v, double* w,
+                                               const double* scal, int t) {
+    double* F[3] = {u, v, w};
+    const GhostCell gc = ghost_cell_of(g, t);
+    const int m = gc.m, side = gc.side;
+    long long cg, cs;
+    if (gc.face == 0) {
+        const int j = gc.j, k = gc.k;
+        cg = g.at(side == 0 ? -m : g.mx - 1 + m, j, k);
+        if (g.xbc != XBC_PER) {
+            double ug, vg, wg;
+            if (g.xbc == XBC_WALL || side == 0) {   // wall or boundary-layer wall: odd
+                const long long cp = g.at(side == 0 ? m - 1 : g.mx - m, j, k);
+                ug = -u[cp]; vg = -v[cp]; wg = -w[cp];
+                double pv;
+                if (g.xbc == XBC_BL && ph.perturbed && wall_perturbation(ph, g.dy, j, k, scal[SC_TIME], &pv)) ug = pv;
+            } else {                                // boundary-layer free stream: extrapolated
+                const long long cl = g.at(g.mx - 1, j, k);
+                const long long cm = g.at(g.mx - 1 - m, j, k);
+                ug = 2.0 * u[cl] - u[cm];
+                vg = 2.0 * v[cl] - v[cm];
+                wg = 2.0 * w[cl] - w[cm];
+            }
+            u[cg] = ug; v[cg] = vg; w[cg] = wg;
+            return;
+        }
+        cs = g.at(side == 0 ? g.mx - m : m - 1, j, k);
+    } else if (gc.face == 1) {
+        cg = g.at(gc.i, side == 0 ? -m : g.my - 1 + m, gc.k);
+        cs = g.at(gc.i, side == 0 ? g.my - m : m - 1, gc.k);
+    } else {
+        cg = g.at(gc.i, gc.j, side == 0 ? -m : g.mz - 1 + m);
+        if (g.zbl) {
+            const long long c0 = g.at(gc.i, gc.j, side == 0 ? 0 : g.mz - 1);
+            const long long cm = g.at(gc.i, gc.j, side == 0 ? m : g.mz - 1 - m);
+            double a[3], b[3];
+#pragma unroll
+            for (int q = 0; q < 3; q++) { a[q] = F[q][c0]; b[q] = F[q][cm]; }
+#pragma unroll
+            for (int q = 0; q < 3; q++) F[q][cg] = 2.0 * a[q] - b[q];
+            return;
+        }
+        cs = g.at(gc.i, gc.j, side == 0 ? g.mz - m : m - 1);
+    }
+    double val[3];
+#pragma unroll
+    for (int q = 0; q < 3; q++) val[q] = F[q][cs];
+#pragma unroll
+    for (int q = 0; q < 3; q++) F[q][cg] = val[q];
+}
+
+// ---------------------------------------------------------------------------------
+// Velocity gradients gij[0..8] = d(u,v,w)/d(x,y,z) at the viscous order and the
+// dilatation (derVelX/Y/Z + calcDil, src/calc_stress.cu:20-63,87-96).
+// ---------------------------------------------------------------------------------
+// DIL_ONLY: only the three diagonal gradients and theta (the FP32-RHS kernel forms the nine
+// gradients itself from the velocity stencils it loads, and needs theta at its neighbours).
 // own: also write the dilatation's ghost images (dil_ghost_owner; periodic and wall x,
-// periodic z only)
+// periodic z only).
 template <typename R, int V, bool DIL_ONLY = false>
 __device__ __forceinline__ void grad_point(const Geom& g, const CoefT<R>& cf, const R* __restrict__ u,
                                            const R* __restrict__ v, const R* __restrict__ w, const GradOut<R>& o,

@@ -61,6 +61,7 @@ SIGNATURES = {
     "cns_probe_fma_peak": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, ctypes.c_int, _dp]),
     "cns_plane_stats": (ctypes.c_int, [_vp, _dp]),
     "cns_friction_reynolds": (ctypes.c_int, [_vp, _dp]),
+    "cns_dissipation": (ctypes.c_int, [_vp, _dp]),
     "cns_selftest_pow": (ctypes.c_int, [ctypes.c_int, _vp, ctypes.c_longlong, ctypes.c_double, _vp, _vp]),
     "cns_selftest_convert": (ctypes.c_int, [ctypes.c_int, _vp, _vp, ctypes.c_longlong, _vp, _vp, _vp, _vp]),
 }

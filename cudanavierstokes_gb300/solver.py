@@ -131,6 +131,13 @@ class Solver:
         native.check(native.lib().cns_friction_reynolds(self._h, _ptr(r)))
         return float(r[0])
 
+    def dissipation(self) -> dict:
+        """Volume-averaged viscous dissipation <tau_ij du_i/dx_j> (`eps`) and enstrophy
+        <|curl u|^2> (`enstrophy`) of the current state, FP64, on the device."""
+        r = np.zeros(2)
+        native.check(native.lib().cns_dissipation(self._h, _ptr(r)))
+        return dict(eps=float(r[0]), enstrophy=float(r[1]))
+
     def scalars(self) -> dict:
         a, b, c = (ctypes.c_double() for _ in range(3))
         native.check(native.lib().cns_get_scalars(self._h, ctypes.byref(a), ctypes.byref(b), ctypes.byref(c)))

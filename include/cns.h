@@ -215,6 +215,13 @@ CNS_API int cns_plane_stats(cns_solver* h, double* out);
  * the advective order from the interior values mirrored evenly about the wall. */
 CNS_API int cns_friction_reynolds(cns_solver* h, double* ret);
 
+/* Volume-averaged viscous dissipation and enstrophy of the current state, in FP64 from the
+ * FP64 state (either precision mode): out[0] = < tau_ij du_i/dx_j >, tau_ij = mu (du_i/dx_j
+ * + du_j/dx_i - 2/3 delta_ij theta), mu = T^viscexp / Re; out[1] = < |curl u|^2 >; means
+ * with the cell volumes over the box, gradients as derVelX/Y/Z (src/calc_stress.cu:20-63)
+ * at the viscous order. The reference computes neither (post-processing). */
+CNS_API int cns_dissipation(cns_solver* h, double* out);
+
 /* Stateless device reductions of a caller-owned state, the reference's calcTimeStep
  * (deviceCalcDt + hostReduceToMin, src/calc_stress.cu:122-160, src/cuda_math.cu:308-333)
  * and the volume integrals of calcPressureGrad / calcBulk (src/calc_stress.cu:98-201,

@@ -838,6 +838,38 @@ double friction_reynolds(const Oracle& o) {
 
 }  // namespace
 
+/* Volume-averaged viscous dissipation <tau_ij du_i/dx_j> and enstrophy <|curl u|^2> of the
+ * current state: the restatement of the library's diagnostic (which the reference leaves
+ * to post-processing) on the reference's own pieces: gradients of derVel
+ * (src/calc_stress.cu:20-63), mu of calcState (src/cuda_main.cu:218-242), cell weights of
+ * the bulk integrals (src/calc_stress.cu:162-201). */
+void dissipation(Oracle& o, double* out) {
+    calcState(o);
+    derVel(o);
+    const int mx = o.mx;
+    const long long N = (long long)o.N;
+    double sp = 0.0, se = 0.0;
+#pragma omp parallel for schedule(static) reduction(+ : sp, se)
+    for (long long gl = 0; gl < N; gl++) {
+        double G[9];
+        for (int q = 0; q < 9; q++) G[q] = o.g[q][gl];   /* G[3 d + n] = d u_n / d x_d */
+        const double th = o.dil[gl];
+        double s = 0.0;
+        for (int d = 0; d < 3; d++)
+            for (int n = 0; n < 3; n++) {
+                double tau = G[3 * d + n] + G[3 * n + d] - (n == d ? 2.0 / 3.0 * th : 0.0);
+                s += tau * G[3 * d + n];
+            }
+        const double wx = G[5] - G[7], wy = G[6] - G[2], wz = G[1] - G[3];
+        const double wv = o.dxv[gl % mx] / o.d_dy / o.d_dz;
+        sp += o.m[gl] * s * wv;
+        se += (wx * wx + wy * wy + wz * wz) * wv;
+    }
+    const double vol = o.p.Lx * o.p.Ly * o.p.Lz;
+    out[0] = sp / vol;
+    out[1] = se / vol;
+}
+
 extern "C" {
 
 const char* cnso_last_error(void) { return g_err; }
@@ -1049,6 +1081,11 @@ int cnso_set_scalars(void* h, double dt, double dpdz, double time) {
 
 int cnso_plane_stats(void* h, double* out) {
     plane_stats(*(Oracle*)h, out);
+    return 0;
+}
+
+int cnso_dissipation(void* h, double* out) {
+    dissipation(*(Oracle*)h, out);
     return 0;
 }
 

@@ -73,6 +73,7 @@ def lib():
         L.cnso_set_scalars.argtypes = [v, ctypes.c_double, ctypes.c_double, ctypes.c_double]
         L.cnso_plane_stats.argtypes = [v, _dp]
         L.cnso_friction_reynolds.argtypes = [v, _dp]
+        L.cnso_dissipation.argtypes = [v, _dp]
         _lib = L
     return _lib
 
@@ -177,6 +178,12 @@ class Oracle:
         r = np.zeros(1)
         lib().cnso_friction_reynolds(self.h, _ptr(r))
         return float(r[0])
+
+    def dissipation(self):
+        """Volume-averaged viscous dissipation and enstrophy (cnso_dissipation)."""
+        r = np.zeros(2)
+        lib().cnso_dissipation(self.h, _ptr(r))
+        return dict(eps=float(r[0]), enstrophy=float(r[1]))
 
     def bulk(self):
         a, b = np.zeros(1), np.zeros(1)

@@ -128,6 +128,26 @@ def test_tgv_kinetic_energy_decays(oracle_mod):
     assert ke1 < k0
 
 
+def test_tgv_initial_dissipation_and_enstrophy(oracle_mod):
+    """Taylor-Green start u = sin x cos y cos z, v = -cos x sin y cos z, w = 0: the mean
+    squared vorticity is 1/8 + 1/8 + 4/8 = 3/4 and, being divergence-free, the viscous
+    dissipation is mu <|curl u|^2> = 3/4 mu with mu = T/Re, T = 1 up to the O(Ma^2)
+    pressure field; the decay rate of K = <rho |u|^2>/2 over the first steps matches it."""
+    p = tgv_params(32)
+    o = oracle_mod.Oracle(p)
+    o.set_state(*tgv_fields(p))
+    d = o.dissipation()
+    assert abs(d["enstrophy"] - 0.75) <= 1e-7
+    assert abs(d["eps"] * p.Re / 0.75 - 1.0) <= 3e-3
+    ke0, _ = o.bulk()                      # <u.u>
+    o.run(20)
+    ke1, _ = o.bulk()
+    t1 = o.scalars()["time"]
+    d1 = o.dissipation()
+    rate = 0.5 * (ke0 - ke1) / t1          # -d(<u.u>/2)/dt over the first steps
+    assert abs(rate / (0.5 * (d["eps"] + d1["eps"])) - 1.0) <= 2e-2
+
+
 def test_quirk_only_affects_energy(oracle_mod):
     p = tgv_params(16)
     f = smooth_random_state(p, seed=8)

@@ -5,9 +5,9 @@ import numpy as np
 import pytest
 
 from cudanavierstokes_gb300 import Solver
-from cudanavierstokes_gb300.params import channel_params
+from cudanavierstokes_gb300.params import PREC_FP32_RHS, PREC_FP64, channel_params, tgv_params
 from tests import golden_cases
-from tests._util import wall_state
+from tests._util import smooth_random_state, wall_state
 
 pytestmark = pytest.mark.gpu
 
@@ -58,3 +58,37 @@ def test_statistics_on_a_perturbed_channel(gpu_lib, oracle_mod):
     st = s.plane_stats()
     assert max(_col_err(st, o.plane_stats(), _uscale(f))) <= 1e-12
     np.testing.assert_array_equal(st[0], o.grid()["x"])
+
+
+def _diss_close(a, b):
+    return all(abs(a[k] - b[k]) <= 1e-12 * abs(b[k]) for k in ("eps", "enstrophy"))
+
+
+@pytest.mark.parametrize("prec", [PREC_FP64, PREC_FP32_RHS])
+@pytest.mark.parametrize("name", golden_cases.names())
+def test_dissipation_matches_oracle(gpu_lib, oracle_mod, name, prec):
+    """Viscous dissipation and enstrophy of the golden cases' start and end fields (periodic
+    box, stretched walls, boundary layer with its perturbed wall ghosts): the FP64
+    diagnostic in either precision mode against the oracle."""
+    case = golden_cases.load(name)
+    p = case["params"]
+    o = oracle_mod.Oracle(p)
+    s = Solver(p.copy(precision=prec))
+    for fields in (case["ic"], case["out"]):
+        o.set_state(*fields)
+        s.copy_field_in(*fields)
+        d, do = s.dissipation(), o.dissipation()
+        assert do["eps"] > 0 and do["enstrophy"] > 0
+        assert _diss_close(d, do), (d, do)
+
+
+def test_dissipation_of_an_evolved_fp32_state(gpu_lib, oracle_mod):
+    """After FP32-RHS steps the diagnostic reads the FP64 state: the oracle on the copied-out
+    state gives the same values."""
+    p = tgv_params(24).copy(my=20, mz=16)
+    s = Solver(p.copy(precision=PREC_FP32_RHS))
+    s.copy_field_in(*smooth_random_state(p, seed=4))
+    s.run(5)
+    o = oracle_mod.Oracle(p)
+    o.set_state(*s.copy_field_out())
+    assert _diss_close(s.dissipation(), o.dissipation())
