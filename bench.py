@@ -295,22 +295,35 @@ def run_serving(args):
 
 def ke_series(p, fields, t_end, chunk=250):
     """Run to t_end logging, every step, the state's time and <u.u>, <rho|u|^2>/2 (the
-    bulk diagnostic is evaluated on the state at the start of each step)."""
+    bulk diagnostic is evaluated on the state at the start of each step); near t_end single
+    steps, with the device's viscous dissipation <tau_ij du_i/dx_j> of the states on either
+    side of t_end, interpolated linearly to t_end."""
     from cudanavierstokes_gb300 import Solver
     s = Solver(p.copy(check_bulk=1))
     s.copy_field_in(*fields)
     t_prev, ts, k1, k2 = 0.0, [], [], []
+    dt = None
     t0 = time.perf_counter()
-    while True:
-        lg = s.run(chunk)
+    diss = []
+    while t_prev < t_end:
+        # chunks that stay short of t_end (dt drifts slowly), then single steps across it
+        n = chunk if dt is None else min(chunk, int(0.98 * (t_end - t_prev) / dt) - 1)
+        single = n < 2
+        if single:
+            diss.append((t_prev, s.dissipation()["eps"]))
+        lg = s.run(1 if single else n)
         tt = np.concatenate([[t_prev], lg["time"][:-1]])
         ts.append(tt); k1.append(lg["par1"]); k2.append(lg["par2"])
+        dt = float(lg["time"][-1] - tt[-1])
         t_prev = float(lg["time"][-1])
-        if t_prev >= t_end:
-            break
+    diss.append((t_prev, s.dissipation()["eps"]))
+    lg = s.run(3)   # samples beyond t_end for the cubic through the 4 around it
+    ts.append(np.concatenate([[t_prev], lg["time"][:-1]])); k1.append(lg["par1"]); k2.append(lg["par2"])
     wall = time.perf_counter() - t0
+    (ta, ea), (tb, eb) = diss[-2], diss[-1]
+    eps_end = ea + (eb - ea) * (t_end - ta) / (tb - ta)
     out = dict(t=np.concatenate(ts), ke=np.concatenate(k1), ke_rho=np.concatenate(k2), wall=wall,
-               steps=int(sum(len(a) for a in ts)))
+               steps=int(sum(len(a) for a in ts)), eps_viscous=eps_end)
     s.close()
     return out
 
@@ -325,8 +338,9 @@ def at_time(t, y, t0):
 
 def run_precision(args):
     """BASELINE config 2: Taylor-Green to t_end, FP32 RHS (FP64 state, accumulation, T/p
-    recovery, reductions) against all-FP64; relative error of <u.u>, <rho|u|^2>/2 and of the
-    dissipation rate eps = -dK/dt at t_end (K = <rho|u|^2>/2)."""
+    recovery, reductions) against all-FP64; relative error of <u.u>, <rho|u|^2>/2, of the
+    dissipation rate eps = -dK/dt at t_end (K = <rho|u|^2>/2) and of the viscous dissipation
+    <tau_ij du_i/dx_j> at t_end (cns_dissipation)."""
     from cudanavierstokes_gb300.initial import tgv_fields
     from cudanavierstokes_gb300.params import tgv_params
     n = int(args.grid.split(",")[0]) if args.grid else 128
@@ -334,7 +348,8 @@ def run_precision(args):
     f = tgv_fields(p64)
     r64 = ke_series(p64, f, args.t_end)
     r32 = ke_series(p64.copy(precision=1), f, args.t_end)
-    res = {}
+    res = {"eps_viscous": {"fp64": r64["eps_viscous"], "fp32_rhs": r32["eps_viscous"],
+                           "rel_err": abs(r32["eps_viscous"] - r64["eps_viscous"]) / abs(r64["eps_viscous"])}}
     for key in ("ke", "ke_rho"):
         a, da = at_time(r64["t"], r64[key], args.t_end)
         b, db = at_time(r32["t"], r32[key], args.t_end)
@@ -344,7 +359,7 @@ def run_precision(args):
             "unit": "relative", "higher_is_better": False, "dtype": "f32-rhs/f64-state vs f64",
             "data": "synthetic", "config": {"workload": f"Taylor-Green {n}^3, Ma 0.1, Re 1600, Pr 0.71, S=V=4, "
                                                         "Wray RK3, CFL 0.5", "t_end": args.t_end},
-            "ke_uu": res["ke"], "ke_rho": res["ke_rho"],
+            "ke_uu": res["ke"], "ke_rho": res["ke_rho"], "eps_viscous": res["eps_viscous"],
             "fp64": {"steps": r64["steps"], "wall_s": r64["wall"],
                      "Mpoint_steps_per_s": p64.npoints * r64["steps"] / r64["wall"] / 1e6},
             "fp32_rhs": {"steps": r32["steps"], "wall_s": r32["wall"],
