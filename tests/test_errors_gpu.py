@@ -40,3 +40,12 @@ def test_unstable_run_reports_nonfinite_state(gpu_lib, prec):
     q.copy_field_in(*tgv_fields(q.p))
     q.run(3)
     assert all(np.isfinite(f).all() for f in q.copy_field_out())
+
+
+def test_statistics_need_a_state(gpu_lib):
+    """The device statistics on a handle with no field copied in return CNS_ERR_STATE."""
+    s = Solver(tgv_params(16))
+    for call in (s.dissipation, s.friction_reynolds, s.plane_stats):
+        with pytest.raises(CnsError) as e:
+            call()
+        assert e.value.code == 6   # CNS_ERR_STATE
