@@ -53,6 +53,15 @@ class Batch:
         self.params[i.value] = p
         return i.value
 
+    def set_member_sponge(self, mid: int, sponge_x, sponge_z, rref, uref, wref, eref) -> None:
+        """The sponge of a member (boundary layer): strengths on x and z, reference fields on
+        the (x, z) plane, as Solver.set_sponge."""
+        h = native.lib().cns_batch_member(self._b, int(mid))
+        if not h:
+            raise native.CnsError(1, "no batch member with this id")
+        a = [np.ascontiguousarray(v, dtype=np.float64) for v in (sponge_x, sponge_z, rref, uref, wref, eref)]
+        native.check(native.lib().cns_set_sponge(h, *[_ptr(v) for v in a]))
+
     def remove(self, mid: int) -> None:
         native.check(native.lib().cns_batch_remove(self._b, int(mid)))
         self.shapes.pop(mid, None)

@@ -10,7 +10,8 @@ import pytest
 from cudanavierstokes_gb300 import Solver
 from cudanavierstokes_gb300.batch import Batch
 from cudanavierstokes_gb300.initial import channel_fields, tgv_fields
-from cudanavierstokes_gb300.params import PREC_FP32_RHS, PREC_FP64, channel_params, tgv_params
+from cudanavierstokes_gb300.params import (PREC_FP32_RHS, PREC_FP64, boundary_layer_params, channel_params,
+                                           tgv_params)
 from tests._util import smooth_random_state, state_errors
 
 pytestmark = pytest.mark.gpu
@@ -87,6 +88,37 @@ def test_membership_changes_between_steps(gpu_lib, mode):
         s.copy_field_in(*f)
         s.run(n)
         assert max(state_errors(bt.fields(mid), s.copy_field_out())) <= 1e-12
+
+
+@pytest.mark.parametrize("mode", MODES)
+@pytest.mark.parametrize("prec", [PREC_FP64, PREC_FP32_RHS])
+def test_boundary_layer_member(gpu_lib, oracle_mod, prec, mode):
+    """A boundary-layer member (sponge, perturbed wall, extrapolated ghosts, time-dependent
+    wall ghosts) next to a periodic one equals its standalone solver."""
+    from oracle.ref_harness import blasius_like_profile
+    p = boundary_layer_params(16, 8, 160, precision=prec, stencil_size=4, stencil_visc=4)   # the batch's orders
+    o = oracle_mod.Oracle(p)
+    spx, spz = o.sponge_strengths()
+    refs = o.sponge_refs(*blasius_like_profile())
+    rref, uref, wref, eref = refs
+    noise = smooth_random_state(p, seed=8, amp=0.01)
+    f = [np.broadcast_to(a[:, None, :], p.shape) * (1.0 + 0.01 * noise[0]) if q in (0, 4) else
+         np.broadcast_to(a[:, None, :], p.shape) + 0.01 * noise[q]
+         for q, a in enumerate((rref, uref, np.zeros_like(rref), wref, eref))]
+    other = members(prec)[0]
+    bt = Batch(precision=prec)
+    bt.set_mode(mode)
+    i0 = bt.add(*other, max_steps=8)
+    ib = bt.add(p, f, max_steps=8)
+    bt.set_member_sponge(ib, spx, spz, rref, uref, wref, eref)
+    bt.step(4)
+    s = Solver(p)
+    s.set_sponge(spx, spz, rref, uref, wref, eref)
+    s.copy_field_in(*f)
+    s.run(4)
+    tol = 1e-12 if prec == PREC_FP64 else 1e-6
+    assert max(state_errors(bt.fields(ib), s.copy_field_out())) <= tol
+    assert bt.steps_done(i0) == 4
 
 
 def test_budget_admission(gpu_lib):
