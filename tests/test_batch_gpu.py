@@ -121,6 +121,23 @@ def test_boundary_layer_member(gpu_lib, oracle_mod, prec, mode):
     assert bt.steps_done(i0) == 4
 
 
+@pytest.mark.parametrize("mode", MODES)
+@pytest.mark.parametrize("S,V", [(1, 1), (2, 2), (3, 2), (4, 1)])
+def test_other_stencil_orders(gpu_lib, S, V, mode):
+    """Batches of other stencil orders (their own kernel instantiations): a periodic box and
+    a channel against standalone solvers, FP64."""
+    ms = [(p.copy(stencil_size=S, stencil_visc=V), f) for p, f in members(PREC_FP64)[1:]]
+    bt = Batch(precision=PREC_FP64, stencil_size=S, stencil_visc=V)
+    bt.set_mode(mode)
+    ids = [bt.add(p, f, max_steps=8) for p, f in ms]
+    bt.step(3)
+    for mid, (p, f) in zip(ids, ms):
+        s = Solver(p)
+        s.copy_field_in(*f)
+        s.run(3)
+        assert max(state_errors(bt.fields(mid), s.copy_field_out())) <= 1e-12
+
+
 def test_budget_admission(gpu_lib):
     p, f = members(PREC_FP64)[0]
     bt = Batch(precision=PREC_FP64, hbm_budget_bytes=1)
