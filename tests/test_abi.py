@@ -52,6 +52,14 @@ def test_parameter_validation(gpu_lib):
         assert gpu_lib.cns_last_error().decode()
 
 
+def test_largest_grids(gpu_lib):
+    """Element offsets are 32-bit: a padded field must hold fewer than 2^31 elements. 1024^3
+    (1.12e9 padded elements) is accepted, 1280^3 (2.16e9) is rejected with a message."""
+    assert gpu_lib.cns_check_params(ctypes.byref(tgv_params(16).copy(mx=1024, my=1024, mz=1024))) == 0
+    assert gpu_lib.cns_check_params(ctypes.byref(tgv_params(16).copy(mx=1280, my=1280, mz=1280))) == 1
+    assert "2^31" in gpu_lib.cns_last_error().decode()
+
+
 def test_create_fails_loudly_without_device(gpu_lib):
     import torch
     if torch.cuda.is_available():
