@@ -8,7 +8,7 @@ import pytest
 
 from cudanavierstokes_gb300 import Solver
 from cudanavierstokes_gb300.initial import channel_fields, tgv_fields
-from cudanavierstokes_gb300.params import (PREC_FP32_RHS, RK3_CLASSIC, RK4_CLASSIC, boundary_layer_params,
+from cudanavierstokes_gb300.params import (PREC_FP32_RHS, PREC_FP64, RK3_CLASSIC, RK4_CLASSIC, boundary_layer_params,
                                            channel_params, tgv_params)
 from tests._util import field_errors, rel_err, smooth_random_state, state_errors, wall_state
 
@@ -245,6 +245,23 @@ def test_fp32_channel_odd_mx(gpu_lib, oracle_mod):
     o.run(3)
     s.run(3)
     assert max(state_errors(s.copy_field_out(), o.get_state())) <= 2e-6
+
+
+@pytest.mark.parametrize("prec", [PREC_FP64, PREC_FP32_RHS])
+def test_rhs_in_band_groups(gpu_lib, oracle_mod, prec):
+    """A plane wide enough (mx = 512) for the RHS kernel to be launched over groups of
+    4-row bands (9 of the 16 bands, then 7): the RHS and two steps against the oracle."""
+    p = channel_params(512, 64, 12)
+    o = oracle_mod.Oracle(p)
+    f = wall_state(p, o.grid()["x"])
+    o.set_state(*f)
+    s = Solver(p.copy(precision=prec))
+    s.copy_field_in(*f)
+    errs = field_errors(s.calc_rhs(), o.rhs())
+    assert max(errs) <= (TOL64 if prec == PREC_FP64 else 1e-4), errs
+    o.run(2)
+    s.run(2)
+    assert max(state_errors(s.copy_field_out(), o.get_state())) <= (TOL64 if prec == PREC_FP64 else 2e-6)
 
 
 def test_rk4_third_order_or_better(gpu_lib):
