@@ -98,9 +98,10 @@ void launch_pack(const Geom& g, const T* src, double* dst, cudaStream_t s);
 // record `msg` as the calling thread's cns_last_error() text and return `code`
 int set_error(int code, const char* msg);
 
-void launch_rhs_fp64(int S, int V, const Geom& g, const Phys& ph, const CoefT<double>& cf, const RhsIn<double>& in,
-                     const Update<double>& up, double* scal, int quirk, cudaStream_t s);
-void launch_rhs_fp32(int S, int V, const Geom& g, const Phys& ph, const CoefT<float>& cf, const RhsIn<float>& in,
-                     const Update<float>& up, double* scal, int quirk, cudaStream_t s);
+// the RHS + stage kernel over the interior; returns the number of launches (band groups)
+int launch_rhs_fp64(int S, int V, const Geom& g, const Phys& ph, const CoefT<double>& cf, const RhsIn<double>& in,
+                    const Update<double>& up, double* scal, int quirk, cudaStream_t s);
+int launch_rhs_fp32(int S, int V, const Geom& g, const Phys& ph, const CoefT<float>& cf, const RhsIn<float>& in,
+                    const Update<float>& up, double* scal, int quirk, cudaStream_t s);
 
 }  // namespace cns

@@ -396,10 +396,11 @@ inline int rhs_band_group(const Geom& g) {
 }
 
 template <typename R>
-void launch_rhs_t(int S, int V, const Geom& g, const CoefT<R>& cf, const RhsIn<R>& in, const Update<R>& up,
-                  double* scal, int quirk, cudaStream_t s) {
+int launch_rhs_t(int S, int V, const Geom& g, const CoefT<R>& cf, const RhsIn<R>& in, const Update<R>& up,
+                 double* scal, int quirk, cudaStream_t s) {
     const int nby = (g.my + 3) / 4, group = rhs_band_group(g);
-    for (int b0 = 0; b0 < nby; b0 += group) {
+    int n = 0;
+    for (int b0 = 0; b0 < nby; b0 += group, n++) {
         dim3 grid((g.mx + 31) / 32, (unsigned)(nby - b0 < group ? nby - b0 : group), g.mz), block(32, 4, 1);
 #define CNS_RHS_CASE(SS, VV) \
     if (S == SS && V == VV) { k_rhs<R, SS, VV><<<grid, block, 0, s>>>(g, cf, in, up, scal, quirk, b0); continue; }
@@ -408,8 +409,9 @@ void launch_rhs_t(int S, int V, const Geom& g, const CoefT<R>& cf, const RhsIn<R
         CNS_RHS_CASE(3, 1) CNS_RHS_CASE(3, 2) CNS_RHS_CASE(3, 3)
         CNS_RHS_CASE(4, 1) CNS_RHS_CASE(4, 2) CNS_RHS_CASE(4, 3) CNS_RHS_CASE(4, 4)
 #undef CNS_RHS_CASE
-        return;   // no instantiation for these orders
+        return n;   // no instantiation for these orders
     }
+    return n;
 }
 
 }  // namespace cns

@@ -2,8 +2,8 @@
 #include "kernels_rhs.cuh"
 
 namespace cns {
-void launch_rhs_fp32(int S, int V, const Geom& g, const Phys&, const CoefT<float>& cf, const RhsIn<float>& in,
-                     const Update<float>& up, double* scal, int quirk, cudaStream_t s) {
-    launch_rhs_t<float>(S, V, g, cf, in, up, scal, quirk, s);
+int launch_rhs_fp32(int S, int V, const Geom& g, const Phys&, const CoefT<float>& cf, const RhsIn<float>& in,
+                    const Update<float>& up, double* scal, int quirk, cudaStream_t s) {
+    return launch_rhs_t<float>(S, V, g, cf, in, up, scal, quirk, s);
 }
 }  // namespace cns

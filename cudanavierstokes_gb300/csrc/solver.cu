@@ -222,13 +222,14 @@ int rhs_phase(cns_solver* h, int kind, double a, double b) {
     const Update<R> up = stage_update<R>(h, kind, a, b, h->cur, kind != ST_RHS_ONLY);
     const int nb = 1 - h->cur;
     const int quirk = h->p.quirk_dissipation_y != 0;
+    int nl;
     if constexpr (std::is_same<R, float>::value)
-        launch_rhs_fp32(h->p.stencil_size, h->p.stencil_visc, h->geom, h->phys, h->cf32, rhs_in<float>(h, h->cur),
-                        up, h->scal, quirk, h->stream);
+        nl = launch_rhs_fp32(h->p.stencil_size, h->p.stencil_visc, h->geom, h->phys, h->cf32, rhs_in<float>(h, h->cur),
+                             up, h->scal, quirk, h->stream);
     else
-        launch_rhs_fp64(h->p.stencil_size, h->p.stencil_visc, h->geom, h->phys, h->cf64, rhs_in<double>(h, h->cur),
-                        up, h->scal, quirk, h->stream);
-    h->launches += 1;
+        nl = launch_rhs_fp64(h->p.stencil_size, h->p.stencil_visc, h->geom, h->phys, h->cf64,
+                             rhs_in<double>(h, h->cur), up, h->scal, quirk, h->stream);
+    h->launches += nl;
     CKL();
     if (kind != ST_RHS_ONLY) {
         // in the reference's program order the latest state recovery before the next
