@@ -134,11 +134,13 @@ __global__ void __launch_bounds__(RED_THREADS) k_reduce_partial(Geom g, Phys ph,
     __shared__ double sh[6][RED_THREADS / 32];
     const long long n = (long long)g.mx * g.my * g.mz;
     double dtmin = 100000.0, s_r = 0.0, s_rw = 0.0, s_e = 0.0, s_k = 0.0, s_rk = 0.0;
+    // 32-bit index arithmetic: n is below the padded field size, itself below 2^31
+    const unsigned mx = (unsigned)g.mx, my = (unsigned)g.my;
     for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x) {
-        const int i = (int)(t % g.mx);
-        const long long jk = t / g.mx;
-        const int j = (int)(jk % g.my);
-        const int k = (int)(jk / g.my);
+        const unsigned tt = (unsigned)t, jk = tt / mx;
+        const int i = (int)(tt - jk * mx);
+        const int j = (int)(jk % my);
+        const int k = (int)(jk / my);
         const long long c = g.at(i, j, k);
         const double rr = q.r[c], uu = q.u[c], vv = q.v[c], ww = q.w[c], ee = q.e[c];
         const double wv = g.wvol[i];
@@ -222,21 +224,22 @@ __global__ void __launch_bounds__(RED_THREADS) k_reduce_final(Phys ph, const dou
 // Layout conversion between the padded device layout and contiguous [k][j][i] arrays.
 // ---------------------------------------------------------------------------------
 template <typename T>
+// (32-bit index arithmetic: the point count is below the padded field size, below 2^31)
 __global__ void __launch_bounds__(256) k_unpack(Geom g, const double* __restrict__ src, T* __restrict__ dst) {
     const long long n = (long long)g.mx * g.my * g.mz;
+    const unsigned mx = (unsigned)g.mx, my = (unsigned)g.my;
     for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x) {
-        const int i = (int)(t % g.mx);
-        const long long jk = t / g.mx;
-        dst[g.at(i, (int)(jk % g.my), (int)(jk / g.my))] = (T)src[t];
+        const unsigned tt = (unsigned)t, jk = tt / mx;
+        dst[g.at((int)(tt - jk * mx), (int)(jk % my), (int)(jk / my))] = (T)src[t];
     }
 }
 template <typename T>
 __global__ void __launch_bounds__(256) k_pack(Geom g, const T* __restrict__ src, double* __restrict__ dst) {
     const long long n = (long long)g.mx * g.my * g.mz;
+    const unsigned mx = (unsigned)g.mx, my = (unsigned)g.my;
     for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x) {
-        const int i = (int)(t % g.mx);
-        const long long jk = t / g.mx;
-        dst[t] = (double)src[g.at(i, (int)(jk % g.my), (int)(jk / g.my))];
+        const unsigned tt = (unsigned)t, jk = tt / mx;
+        dst[t] = (double)src[g.at((int)(tt - jk * mx), (int)(jk % my), (int)(jk / my))];
     }
 }
 
