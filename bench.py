@@ -45,6 +45,7 @@ if REPO not in sys.path:
 METRIC = "Mpoint-steps/s"
 PEAKS_FILE = os.path.join(REPO, "MEASURED_PEAKS.json")
 TRAFFIC_FILE = os.path.join(REPO, "profiles", "rhs_kernel_channel_traffic.txt")
+TRAFFIC_FILE_FP32 = os.path.join(REPO, "profiles", "rhs_kernel_channel_fp32_traffic.txt")
 SLAB_MZ = 24   # CPU sample: full x-y cross-section, 24 streamwise planes
 
 
@@ -367,19 +368,19 @@ def run_precision(args):
     print(json.dumps(line), flush=True)
 
 
-def read_profile_summary():
-    """Key: value lines of the committed ncu summary of the RHS kernel (FP64 channel)."""
+def read_profile_summary(path=TRAFFIC_FILE):
+    """Key: value lines of a committed ncu summary of the RHS kernel (FP64 channel by default)."""
     try:
-        with open(TRAFFIC_FILE) as f:
+        with open(path) as f:
             return {k.strip(): v.strip() for k, v in (line.split(":", 1) for line in f if ":" in line)}
     except Exception:
         return {}
 
 
-def read_traffic(N: int):
-    """Per-launch DRAM bytes of the RHS kernel from the committed ncu summary (scaled to this
-    grid by points if the capture was taken on a smaller case)."""
-    kv = read_profile_summary()
+def read_traffic(N: int, fp32: bool = False):
+    """Per-launch DRAM bytes of the RHS kernel from the committed ncu summary of its precision
+    (scaled to this grid by points if the capture was taken on a smaller case)."""
+    kv = read_profile_summary(TRAFFIC_FILE_FP32 if fp32 else TRAFFIC_FILE)
     try:
         return float(kv["dram_bytes_per_launch"]) * N / float(kv["points"])
     except Exception:
@@ -463,7 +464,7 @@ def run_gb300(args, world, rank, local):
         hbm_src = "measured (MEASURED_PEAKS.json)"
     except Exception:
         hbm_peak, hbm_src = 6800.0, "fallback"
-    traffic = read_traffic(N)
+    traffic = read_traffic(N, fp32=args.precision == "fp32")
     roof = {"bound": "fp64" if args.precision == "fp64" else "fp32", "kernel": "k_rhs (RHS x/y/z + body force + "
             "sponge + RK stage update)", "achieved": ach_tf, "peak": t64.value, "unit": "TFLOP/s",
             "frac": ach_tf / t64.value, "peak_source": "measured live (FMA-chain probe, cns_probe_fma_peak)",
