@@ -277,13 +277,13 @@ void launch_grad(int V, const Geom& g, const CoefT<R>& cf, const R* u, const R* 
         case 3: k_dil_pair<3><<<grid, point_block(), 0, s>>>(g, cf, u, v, w, o.dil, own); break;
         default: k_dil_pair<4><<<grid, point_block(), 0, s>>>(g, cf, u, v, w, o.dil, own); break;
         }
-        return;
-    }
-    switch (V) {
-    case 1: k_grad<R, 1><<<point_grid(g), point_block(), 0, s>>>(g, cf, u, v, w, o, own); break;
-    case 2: k_grad<R, 2><<<point_grid(g), point_block(), 0, s>>>(g, cf, u, v, w, o, own); break;
-    case 3: k_grad<R, 3><<<point_grid(g), point_block(), 0, s>>>(g, cf, u, v, w, o, own); break;
-    default: k_grad<R, 4><<<point_grid(g), point_block(), 0, s>>>(g, cf, u, v, w, o, own); break;
+    } else {
+        switch (V) {
+        case 1: k_grad<R, 1><<<point_grid(g), point_block(), 0, s>>>(g, cf, u, v, w, o, own); break;
+        case 2: k_grad<R, 2><<<point_grid(g), point_block(), 0, s>>>(g, cf, u, v, w, o, own); break;
+        case 3: k_grad<R, 3><<<point_grid(g), point_block(), 0, s>>>(g, cf, u, v, w, o, own); break;
+        default: k_grad<R, 4><<<point_grid(g), point_block(), 0, s>>>(g, cf, u, v, w, o, own); break;
+        }
     }
 }
 template <typename R>
