@@ -4,9 +4,11 @@
 //   [every check_cfl / check_bulk steps: one fused two-pass reduction for dt, the body
 //    force controller and the bulk diagnostics, all on the device]
 //   k_advance_time, then per Runge-Kutta stage:
-//     k_ghost_state -> k_grad (9 gradients + theta) -> k_ghost_scalar (theta)
-//     -> k_rhs (RHS of x, y, z + body force + sponge + update, and T, p, H, mu of the new
-//        state for the next stage; k_state runs only after the state is set from outside)
+//     k_ghost_state -> k_grad (9 gradients + theta; FP32-RHS: k_dil_pair, theta only; both
+//     write theta's ghost images on periodic and wall boundaries, the boundary layer adds
+//     k_ghost_scalar) -> k_rhs (RHS of x, y, z + body force + sponge + update, and T, p, H,
+//     mu of the new state for the next stage; on large planes one launch per group of
+//     bands; k_state runs only after the state is set from outside)
 // with no host round trip inside a run (the reference copies dt and dpdz through the
 // host and MPI every check_cfl steps: src/cuda_main.cu:249-265).
 #include <cuda_runtime.h>
