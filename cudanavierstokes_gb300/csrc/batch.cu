@@ -177,8 +177,7 @@ int upload_table(cns_batch* b) {
         cns_solver* h = b->members[q].h;
         tab[q] = make_inst<R>(h, b->members[q].cap);
         const long long pu = (long long)tab[q].nbx * tab[q].nby * h->p.mz;
-        long long gc = 2LL * h->geom.G *
-                       ((long long)h->p.my * h->p.mz + (long long)h->p.mx * h->p.mz + (long long)h->p.mx * h->p.my);
+        const long long gc = ghost_count(h->geom);   // the ghost phases' cell count
         ctl.unit_off[q + 1] = ctl.unit_off[q] + pu;
         ctl.ghost_off[q + 1] = ctl.ghost_off[q] + (gc + BATCH_THREADS - 1) / BATCH_THREADS;
     }
