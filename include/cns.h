@@ -257,9 +257,12 @@ CNS_API int cns_reduce_state_noalloc(int mx, int my, int mz, const double* r, co
 /* ---------------------------------------------------------------------------------------
  * Batched ensemble (no counterpart in the reference, which runs one simulation per
  * executable): many simulations of different grid sizes and physical parameters that
- * share the stencil orders, the precision and the Wray RK3 scheme advance together, one
- * persistent cooperative kernel launch per Runge-Kutta stage for the whole batch, the
- * step replayed from a captured CUDA graph. Members keep their own dt (CFL), body
+ * share the stencil orders, the precision and the Wray RK3 scheme advance together: one
+ * persistent cooperative kernel launch per Runge-Kutta stage for the whole batch, or each
+ * member's own step graph on one of CNS_BATCH_LANES concurrent streams (the execution
+ * mode, chosen by cns_batch_tune), the step replayed from captured CUDA graphs. A member's
+ * handle (cns_batch_member) takes per-member settings such as its sponge. Members keep
+ * their own dt (CFL), body
  * force, bulk schedule, time and per-step logs. Membership may change between steps
  * (continuous batching); admission respects an optional HBM budget.
  * ------------------------------------------------------------------------------------- */
