@@ -385,7 +385,8 @@ __global__ void __launch_bounds__(128, sizeof(R) == 4 ? 7 : 4) k_rhs(Geom g, Coe
 // stencil inputs of the FP64 kernel; twice the FP32 kernel's, whose other traffic streams
 // through L2 alongside) fit in half of L2, else the largest group that does (at least 8
 // bands). Measured on a 512^3 channel, FP32 RHS step: one launch 45.1 ms, groups of 75
-// bands 38.6, 37 bands 36.9, 18 bands 36.9, 9 bands 37.3 ms; the FP64 step is the same
+// bands 38.6, 37 bands 36.9, 18 bands 36.9, 9 bands 37.3 ms; on 256^3 one launch (this
+// rule) 4.64 ms, groups of 37 bands 4.69, 18 bands 4.74 ms; the FP64 step is the same
 // either way (FP64-pipe bound).
 inline int rhs_band_group(const Geom& g) {
     const int nby = (g.my + 3) / 4;
