@@ -36,6 +36,15 @@ def test_rhs_periodic_all_orders(gpu_lib, oracle_mod, S, V):
     assert max(errs) <= TOL64, errs
 
 
+@pytest.mark.parametrize("S,V", SV)
+def test_rhs_all_orders_odd_edges(gpu_lib, oracle_mod, S, V):
+    """Odd, unequal edges (partial blocks in x and y) at every stencil order, FP64."""
+    p = tgv_params(17).copy(my=13, mz=11, stencil_size=S, stencil_visc=V)
+    o, s = _pair(oracle_mod, p, smooth_random_state(p, seed=100 + S * 10 + V))
+    errs = field_errors(s.calc_rhs(), o.rhs())
+    assert max(errs) <= TOL64, errs
+
+
 @pytest.mark.parametrize("S,V", [(4, 4), (3, 2), (2, 1)])
 def test_rhs_channel_walls(gpu_lib, oracle_mod, S, V):
     p = channel_params(24, 16, 20).copy(stencil_size=S, stencil_visc=V)
@@ -229,6 +238,38 @@ def test_fp32_rhs_all_orders_odd_edges(gpu_lib, oracle_mod, S, V):
     s.copy_field_in(*f)
     errs = field_errors(s.calc_rhs(), o.rhs())
     assert max(errs) <= 2e-5, errs
+
+
+def test_fp32_classic_rk3_against_fp64_oracle(gpu_lib, oracle_mod):
+    """The classic RK3 stages (k1, k2 registers in FP32, the state in FP64) with dt
+    recomputed during the run, FP32-RHS against the FP64 oracle."""
+    p = tgv_params(16).copy(my=20, mz=24, scheme=RK3_CLASSIC, check_cfl=2)
+    f = smooth_random_state(p, seed=12)
+    o = oracle_mod.Oracle(p)
+    o.set_state(*f)
+    s = Solver(p.copy(precision=PREC_FP32_RHS))
+    s.copy_field_in(*f)
+    o.run(5)
+    s.run(5)
+    assert max(state_errors(s.copy_field_out(), o.get_state())) <= 2e-6
+
+
+def test_fp32_boundary_layer_against_fp64_oracle(gpu_lib, oracle_mod):
+    """Boundary layer (sponge, perturbed wall, extrapolated ghosts) in FP32-RHS mode: four
+    steps against the FP64 oracle."""
+    p = boundary_layer_params(16, 8, 160)
+    o, s64 = _bl_setup(oracle_mod, p)
+    f = o.get_state()
+    s = Solver(p.copy(precision=PREC_FP32_RHS))
+    spx, spz = o.sponge_strengths()
+    from oracle.ref_harness import blasius_like_profile
+    rref, uref, wref, eref = o.sponge_refs(*blasius_like_profile())
+    s.set_sponge(spx, spz, rref, uref, wref, eref)
+    s.copy_field_in(*f)
+    o.run(4)
+    s.run(4)
+    assert max(state_errors(s.copy_field_out(), o.get_state())) <= 2e-6
+    del s64
 
 
 def test_fp32_channel_odd_mx(gpu_lib, oracle_mod):
