@@ -208,3 +208,38 @@ def test_rejects_bad_parameters(oracle_mod):
         oracle_mod.Oracle(tgv_params(16).copy(stencil_visc=5))
     with pytest.raises(ValueError):
         oracle_mod.Oracle(tgv_params(4))
+
+
+def test_channel_rhs_mirror_symmetry(oracle_mod):
+    """The stretched channel is symmetric about its mid-plane: a state mirrored in x with
+    the wall-normal velocity reversed has the mirrored RHS, with the wall-normal momentum
+    term reversed (walls, stretched-grid metrics and fluxes treat both halves alike)."""
+    from tests._util import wall_state
+    p = channel_params(24, 12, 16)
+    o = oracle_mod.Oracle(p)
+    x = o.grid()["x"]
+    assert np.allclose(x + x[::-1], p.Lx, atol=1e-13)
+    f = wall_state(p, x, seed=5)
+    o.set_state(*f)
+    a = o.rhs()
+    m = [g[:, :, ::-1].copy() for g in f]
+    m[1] = -m[1]
+    o.set_state(*m)
+    b = o.rhs()
+    for q in range(5):
+        ref = -a[q][:, :, ::-1] if q == 1 else a[q][:, :, ::-1]
+        assert np.max(np.abs(b[q] - ref)) <= 1e-13 * np.max(np.abs(a[q])), q
+
+
+def test_periodic_shift_invariance(oracle_mod):
+    """Shifting a periodic state by one cell in y (and in z) shifts its RHS bit for bit."""
+    p = tgv_params(12).copy(my=10, mz=14)
+    o = oracle_mod.Oracle(p)
+    f = smooth_random_state(p, seed=9)
+    o.set_state(*f)
+    a = o.rhs()
+    for axis in (1, 0):   # y, then z ([k][j][i] arrays)
+        o.set_state(*[np.roll(g, 1, axis=axis) for g in f])
+        b = o.rhs()
+        for q in range(5):
+            assert np.array_equal(b[q], np.roll(a[q], 1, axis=axis)), (axis, q)
