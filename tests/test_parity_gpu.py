@@ -378,3 +378,26 @@ def test_fp32_rhs_stage_kinds_run_alike(gpu_lib):
     first = min(s.time_phases(1)["rhs_ms"] for _ in range(3))
     avg = min(s.time_phases(3)["rhs_ms"] for _ in range(3))
     assert avg <= 1.5 * first, (first, avg)
+
+
+def test_gpu_rhs_mirror_and_shift(gpu_lib):
+    """Independent of the oracle: the channel RHS of a state mirrored in x (wall-normal
+    velocity reversed) is the mirrored RHS, and a periodic shift by one cell in y shifts
+    the RHS bit for bit."""
+    p = channel_params(24, 12, 16)
+    s = Solver(p)
+    x = s.grid()["x"]
+    f = wall_state(p, x, seed=5)
+    s.copy_field_in(*f)
+    a = s.calc_rhs()
+    m = [g[:, :, ::-1].copy() for g in f]
+    m[1] = -m[1]
+    s.copy_field_in(*m)
+    b = s.calc_rhs()
+    for q in range(5):
+        ref = -a[q][:, :, ::-1] if q == 1 else a[q][:, :, ::-1]
+        assert np.max(np.abs(b[q] - ref)) <= 1e-13 * np.max(np.abs(a[q])), q
+    s.copy_field_in(*[np.roll(g, 1, axis=1) for g in f])
+    c = s.calc_rhs()
+    for q in range(5):
+        assert np.array_equal(c[q], np.roll(a[q], 1, axis=1)), q
