@@ -12,23 +12,33 @@ reference itself. Steps:
           which CUDA >= 12 rejects) in `#if 0`, write the initial fields as restart
           files fields/*.0000000.bin (or, for the boundary layer, synthetic self-similar
           profiles blasius1D/*.bin) and a Makefile.
+          Cases at the benchmark sizes (the 64^3 Taylor-Green box and the 128x160x192
+          channel) stage no field files: their initial fields are written on the run
+          host, from the same seeded generators, just before the reference runs.
   run     (on a GB300 host) `make` each case for sm_103a and run ./ns with
           CUDA_LAUNCH_BLOCKING=1 (program order: the reference's streams race otherwise),
           then pack initial and final fields, the dt/dpdz log, the friction Reynolds
           number the reference prints for the initial field (printRes) and its prof.txt
-          plane profiles of the final field (calcAvgChan) into
-          <OUT_ROOT>/<case>.npz.
-  collect (back on the machine with the checkout) copy the packed results to
-          tests/golden/.
+          plane profiles of the final field (calcAvgChan) into <out>/<case>.npz. For the
+          benchmark-size cases the fields are packed as a strided subsample plus, per
+          field, the maximum magnitude and the plane sums along each axis over the whole
+          grid (tests/golden stays a few MB).
+  collect (back on the machine with the checkout) copy the packed results from <out>
+          to tests/golden/ (ref_<case>.npz; benchmark-size cases refsub_<case>.npz).
 
   time    (on a GB300 host) build and run the staged timing cases (the benchmark
           channel at two run lengths) and write the reference's per-step time to
-          <OUT_ROOT>/ref_timing.json.
+          <out>/ref_timing.json.
 
-Usage: python oracle/ref_harness.py {stage|run|time|collect} [case ...]
+The reference checkout is taken from $CNS_REFERENCE_ROOT, else from the default checkout
+location below; <out> is the --out directory the caller names.
+
+Usage: python oracle/ref_harness.py stage [case ...]
+       python oracle/ref_harness.py {run|time|collect} --out DIR [case ...]
 """
 from __future__ import annotations
 
+import argparse
 import json
 import math
 import os
@@ -44,14 +54,19 @@ REPO = os.path.dirname(HERE)
 sys.path.insert(0, REPO)
 
 from cudanavierstokes_gb300.params import (  # noqa: E402
-    RK3_CLASSIC, RK3_LOWSTORAGE, boundary_layer_params, channel_params, tgv_params)
+    RK3_CLASSIC, RK3_LOWSTORAGE, CnsParams, boundary_layer_params, channel_params, tgv_params)
 from cudanavierstokes_gb300 import initial  # noqa: E402
 
-REF_SRC = "/root/reference/src"
+DEFAULT_REFERENCE_ROOT = "/root/reference"
 STAGE_ROOT = os.path.join(HERE, "_ref")
-# results of the runs on the GB300 host, in the folder whose contents come back from it
-OUT_ROOT = os.path.join(REPO, "gpurun_out", "ref_golden")
 GOLDEN = os.path.join(REPO, "tests", "golden")
+
+
+def reference_root():
+    """The reference checkout ($CNS_REFERENCE_ROOT, else the default location), or None
+    when it is absent (a GPU host only has the staged copies under oracle/_ref)."""
+    root = os.environ.get("CNS_REFERENCE_ROOT", DEFAULT_REFERENCE_ROOT)
+    return root if os.path.isdir(os.path.join(root, "src")) else None
 
 
 def cases():
@@ -73,6 +88,17 @@ def cases():
         "channel_24x16x16_s4v4": dict(params=channel_params(24, 16, 16), nsteps=5, ic="channel"),
         # boundary layer: extrapolated x top / z ends, sponge, wall perturbation
         "bl_16x8x160_s3v2": dict(params=boundary_layer_params(16, 8, 160), nsteps=6, ic="bl"),
+    }
+
+
+def large_cases():
+    """Golden cases at the benchmark sizes, 10 steps each: the 64^3 Taylor-Green box (the
+    analytic start with rho = 1) and the 128x160x192 isothermal channel (seeded start), as
+    the benchmark configures them. Their fields are packed as a subsample with stride `sub`
+    plus whole-grid maxima and plane sums."""
+    return {
+        "tgv_64_s4v4": dict(params=tgv_params(64), nsteps=10, ic="tgv", sub=2),
+        "channel_128x160x192_s4v4": dict(params=channel_params(128, 160, 192), nsteps=10, ic="channel", sub=4),
     }
 
 
@@ -213,10 +239,22 @@ def blasius_like_profile(n: int = 601, xmax: float = 60.0):
     return x, r, u, w, e
 
 
+def initial_fields(ic: str, p):
+    """The initial fields of a staged case (written as restart files fields/*.0000000.bin)."""
+    if ic == "tgv":
+        return initial.tgv_fields(p)
+    if ic == "tgv_ref":
+        return initial.tgv_reference_fields(p)
+    from oracle.oracle import Oracle  # grid of the stretched channel
+    return initial.channel_fields(p, Oracle(p).grid()["x"], seed=0)
+
+
 def stage(names):
-    if not os.path.isdir(REF_SRC):
-        raise SystemExit(f"reference sources not found at {REF_SRC}")
-    allc = dict(cases(), **timing_cases())
+    root = reference_root()
+    if root is None:
+        raise SystemExit("reference checkout not found: set CNS_REFERENCE_ROOT")
+    ref_src = os.path.join(root, "src")
+    allc = dict(cases(), **large_cases(), **timing_cases())
     for name in names or cases():
         c = allc[name]
         p, nsteps = c["params"], c["nsteps"]
@@ -225,9 +263,9 @@ def stage(names):
             shutil.rmtree(d)
         os.makedirs(os.path.join(d, "src"))
         os.makedirs(os.path.join(d, "fields"))
-        for fn in os.listdir(REF_SRC):
+        for fn in os.listdir(ref_src):
             if fn.endswith((".cu", ".cpp", ".h")) and fn != "globals.h" and fn != "cuda_derivs.cu":
-                shutil.copy(os.path.join(REF_SRC, fn), os.path.join(d, "src", fn))
+                shutil.copy(os.path.join(ref_src, fn), os.path.join(d, "src", fn))
         cm = os.path.join(d, "src", "cuda_math.cu")
         with open(cm) as f:
             txt = f.read()
@@ -239,29 +277,33 @@ def stage(names):
             f.write(parameter_header(p, nsteps, restart))
         with open(os.path.join(d, "Makefile"), "w") as f:
             f.write(MAKEFILE)
-        if c["ic"] == "ref_init":
+        deferred = "sub" in c
+        if c["ic"] == "ref_init" or deferred:
             pass
         elif c["ic"] == "bl":
             os.makedirs(os.path.join(d, "blasius1D"))
             for nm, arr in zip("xruwe", blasius_like_profile()):
                 arr.astype(np.float64).tofile(os.path.join(d, "blasius1D", f"{nm}Prof.bin"))
         else:
-            if c["ic"] == "tgv":
-                fields = initial.tgv_fields(p)
-            elif c["ic"] == "tgv_ref":
-                fields = initial.tgv_reference_fields(p)
-            else:
-                from oracle.oracle import Oracle  # grid of the stretched channel
-                fields = initial.channel_fields(p, Oracle(p).grid()["x"], seed=0)
-            initial.write_fields(os.path.join(d, "fields"), 0, fields)
+            initial.write_fields(os.path.join(d, "fields"), 0, initial_fields(c["ic"], p))
         with open(os.path.join(d, "case.json"), "w") as f:
-            json.dump(dict(name=name, nsteps=nsteps, ic=c["ic"], params=p.as_dict()), f, indent=1)
+            json.dump(dict(name=name, nsteps=nsteps, ic=c["ic"], params=p.as_dict(), sub=c.get("sub", 0)),
+                      f, indent=1)
         print("staged", d)
 
 
-def run(names):
-    os.makedirs(OUT_ROOT, exist_ok=True)
-    dirs = sorted(n for n in os.listdir(STAGE_ROOT) if os.path.isdir(os.path.join(STAGE_ROOT, n)) and n in cases())
+def pack_large(out, sub: int) -> dict:
+    """A strided subsample of the fields (every `sub`-th point per axis, from 0) and, per
+    field over the whole grid, the maximum magnitude and the plane sums along z, y and x."""
+    a = np.stack(out)
+    return dict(out_sub=np.ascontiguousarray(a[:, ::sub, ::sub, ::sub]), out_absmax=np.abs(a).max(axis=(1, 2, 3)),
+                out_sum_k=a.sum(axis=(2, 3)), out_sum_j=a.sum(axis=(1, 3)), out_sum_i=a.sum(axis=(1, 2)))
+
+
+def run(names, out_root):
+    os.makedirs(out_root, exist_ok=True)
+    known = dict(cases(), **large_cases())
+    dirs = sorted(n for n in os.listdir(STAGE_ROOT) if os.path.isdir(os.path.join(STAGE_ROOT, n)) and n in known)
     ok = True
     for name in dirs:
         if names and name not in names:
@@ -279,10 +321,16 @@ def run(names):
             print(f"[{name}] build failed:\n{b.stdout[-3000:]}\n{b.stderr[-3000:]}")
             ok = False
             continue
+        sub = int(meta.get("sub", 0))
+        pr = CnsParams()
+        for k, v in meta["params"].items():
+            setattr(pr, k, v)
+        if sub:   # benchmark-size case: the initial fields are written here
+            initial.write_fields(os.path.join(d, "fields"), 0, initial_fields(meta["ic"], pr))
         env = dict(os.environ, CUDA_LAUNCH_BLOCKING="1")
         r = subprocess.run(["./ns"], cwd=d, capture_output=True, text=True, env=env, timeout=600)
         log = r.stdout + r.stderr
-        with open(os.path.join(OUT_ROOT, name + ".log"), "w") as f:
+        with open(os.path.join(out_root, name + ".log"), "w") as f:
             f.write(log)
         if r.returncode != 0:
             print(f"[{name}] run failed rc={r.returncode}\n{log[-2000:]}")
@@ -298,21 +346,25 @@ def run(names):
         ret = np.array([float(m.group(1)) if m else np.nan])
         prof_path = os.path.join(d, "prof.txt")
         prof = np.loadtxt(prof_path) if os.path.exists(prof_path) else np.zeros((0, 11))
-        np.savez_compressed(os.path.join(OUT_ROOT, name + ".npz"),
-                            ic=np.stack(ic), out=np.stack(out),
-                            x=np.fromfile(os.path.join(d, "fields", "x.bin")),
-                            steplog=np.array(steps, dtype=np.float64).reshape(-1, 3),
-                            ret=ret, prof=prof, meta=json.dumps(meta))
+        common = dict(x=np.fromfile(os.path.join(d, "fields", "x.bin")),
+                      steplog=np.array(steps, dtype=np.float64).reshape(-1, 3), ret=ret, prof=prof,
+                      meta=json.dumps(meta))
+        if sub:
+            np.savez_compressed(os.path.join(out_root, name + ".npz"),
+                                ic_sub=np.ascontiguousarray(np.stack(ic)[:, ::sub, ::sub, ::sub]),
+                                **pack_large(out, sub), **common)
+        else:
+            np.savez_compressed(os.path.join(out_root, name + ".npz"), ic=np.stack(ic), out=np.stack(out), **common)
         print(f"[{name}] ok: {len(steps)} dt lines, rho range {out[0].min():.6f}..{out[0].max():.6f}")
     return ok
 
 
-def time_runs(names):
+def time_runs(names, out_root):
     """Build and run the staged timing cases twice each: in the reference's native stream
     order (its default, unsynchronised) and with CUDA_LAUNCH_BLOCKING=1 (program order),
-    and write the per-step times and Mpoint-steps/s to <OUT_ROOT>/ref_timing.json."""
+    and write the per-step times and Mpoint-steps/s to <out>/ref_timing.json."""
     tc = timing_cases()
-    os.makedirs(OUT_ROOT, exist_ok=True)
+    os.makedirs(out_root, exist_ok=True)
     res = {}
     for name in sorted(tc):
         if names and name not in names:
@@ -331,7 +383,7 @@ def time_runs(names):
                 r = subprocess.run(["./ns"], cwd=d, capture_output=True, text=True,
                                    env=dict(os.environ, **extra), timeout=900)
                 log = r.stdout + r.stderr
-                with open(os.path.join(OUT_ROOT, f"{name}_{mode}.log"), "w") as f:
+                with open(os.path.join(out_root, f"{name}_{mode}.log"), "w") as f:
                     f.write(log)
                 m = re.search(r"The total time is:\s+(\S+)", log)
                 if r.returncode != 0 or not m:
@@ -352,31 +404,40 @@ def time_runs(names):
             if a and b:
                 per = (b["total_s"] - a["total_s"]) / (b["nsteps"] - a["nsteps"])
                 out.setdefault(fam, {})[mode] = dict(s_per_step=per, mpoint_steps_per_s=pts / per / 1e6)
-    os.makedirs(OUT_ROOT, exist_ok=True)
-    with open(os.path.join(OUT_ROOT, "ref_timing.json"), "w") as f:
+    with open(os.path.join(out_root, "ref_timing.json"), "w") as f:
         json.dump(out, f, indent=1)
     print(json.dumps(out))
     return True
 
 
-def collect(names):
+def collect(names, out_root):
     os.makedirs(GOLDEN, exist_ok=True)
-    for fn in sorted(os.listdir(OUT_ROOT)):
+    large = large_cases()
+    for fn in sorted(os.listdir(out_root)):
         if fn.endswith(".npz") and (not names or fn[:-4] in names):
-            shutil.copy(os.path.join(OUT_ROOT, fn), os.path.join(GOLDEN, "ref_" + fn))
+            prefix = "refsub_" if fn[:-4] in large else "ref_"
+            shutil.copy(os.path.join(out_root, fn), os.path.join(GOLDEN, prefix + fn))
             print("collected", fn)
 
 
+def main(argv):
+    ap = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawDescriptionHelpFormatter)
+    ap.add_argument("cmd", choices=["stage", "run", "time", "collect"])
+    ap.add_argument("cases", nargs="*")
+    ap.add_argument("--out", help="directory of the packed results (run, time, collect)")
+    a = ap.parse_intermixed_args(argv)
+    if a.cmd == "stage":
+        stage(a.cases)
+        return 0
+    if not a.out:
+        ap.error(f"{a.cmd} needs --out DIR")
+    if a.cmd == "run":
+        return 0 if run(a.cases, a.out) else 1
+    if a.cmd == "time":
+        return 0 if time_runs(a.cases, a.out) else 1
+    collect(a.cases, a.out)
+    return 0
+
+
 if __name__ == "__main__":
-    cmd = sys.argv[1] if len(sys.argv) > 1 else "stage"
-    names = sys.argv[2:]
-    if cmd == "stage":
-        stage(names)
-    elif cmd == "run":
-        sys.exit(0 if run(names) else 1)
-    elif cmd == "time":
-        sys.exit(0 if time_runs(names) else 1)
-    elif cmd == "collect":
-        collect(names)
-    else:
-        raise SystemExit(__doc__)
+    sys.exit(main(sys.argv[1:]))

@@ -4,7 +4,9 @@ stand-in modules, since matplotlib is not installed and the function draws nothi
 scratch directory and store the blasius1D/*Prof.bin it writes in
 tests/golden/blasius_ref_profiles.npz.
 
-Run in a checkout next to the reference: python tests/golden/make_blasius_golden.py
+Run in a checkout next to the reference (its location: $CNS_REFERENCE_ROOT, else the
+default checkout location the parity harness uses):
+    python tests/golden/make_blasius_golden.py
 """
 import importlib.util
 import os
@@ -14,11 +16,17 @@ import types
 
 import numpy as np
 
-REF = "/root/reference/python-utils/selfSimilarSol.py"
-OUT = os.path.join(os.path.dirname(os.path.abspath(__file__)), "blasius_ref_profiles.npz")
+HERE = os.path.dirname(os.path.abspath(__file__))
+OUT = os.path.join(HERE, "blasius_ref_profiles.npz")
 
 
 def main():
+    sys.path.insert(0, os.path.dirname(os.path.dirname(HERE)))
+    from oracle.ref_harness import reference_root
+    root = reference_root()
+    if root is None:
+        raise SystemExit("reference checkout not found: set CNS_REFERENCE_ROOT")
+    ref = os.path.join(root, "python-utils", "selfSimilarSol.py")
     mpl = types.ModuleType("matplotlib")
     mpl.rc = lambda *a, **k: None
     mpl.rcParams = {}
@@ -26,7 +34,7 @@ def main():
     mpl.pyplot = plt
     sys.modules.setdefault("matplotlib", mpl)
     sys.modules.setdefault("matplotlib.pyplot", plt)
-    spec = importlib.util.spec_from_file_location("ref_self_similar", REF)
+    spec = importlib.util.spec_from_file_location("ref_self_similar", ref)
     mod = importlib.util.module_from_spec(spec)
     spec.loader.exec_module(mod)
     cwd = os.getcwd()

@@ -43,3 +43,25 @@ def test_oracle_statistics_match_reference(oracle_mod, name):
     prof = o.plane_stats().T
     assert prof.shape == case["prof"].shape
     assert np.abs(prof - case["prof"]).max() <= 5.01e-7
+
+
+@pytest.mark.parametrize("name", golden_cases.large_names())
+def test_oracle_matches_reference_at_benchmark_size(oracle_mod, name):
+    """The benchmark workloads themselves (64^3 Taylor-Green, 128x160x192 channel), 10 steps
+    of the unmodified reference: the oracle's final fields against the reference's
+    subsample and whole-grid plane sums, and the printed dt sequence."""
+    c = golden_cases.load_large(name)
+    p = c["params"]
+    o = oracle_mod.Oracle(p)
+    x = o.grid()["x"]
+    np.testing.assert_allclose(x, c["x"], rtol=0, atol=1e-14)
+    ic = golden_cases.initial_fields(c, x)
+    s = c["sub"]
+    for a, b in zip(ic, c["ic_sub"]):
+        np.testing.assert_allclose(a[::s, ::s, ::s], b, rtol=0, atol=1e-14 * max(1.0, float(np.abs(b).max())))
+    o.set_state(*ic)
+    logs = o.run(c["nsteps"])
+    errs = golden_cases.large_errors(o.get_state(), c)
+    assert max(errs) <= TOL, errs
+    for step, dt, _ in c["steplog"]:
+        assert abs(logs["dt"][int(step)] - dt) <= 5e-7 * dt
