@@ -3,7 +3,8 @@
  *
  * CPU restatement of the CudaNavierStokes time-advance path (state recovery,
  * velocity gradients, dilatation, split-form RHS in x/y/z with boundary conditions,
- * sponge, body force, CFL dt, bulk diagnostics, Wray low-storage RK3 and classic RK3).
+ * sponge, body force, CFL dt, bulk diagnostics, Wray low-storage RK3 and classic RK3),
+ * plus a textbook classic RK4 that has no reference counterpart (rk4Step).
  * It is the parity reference for the GPU library and the timed CPU baseline. It follows
  * the reference kernels line by line, including their arithmetic order, the
  * double-interface flux loops and the y viscous-dissipation quirk, and processes
@@ -686,6 +687,46 @@ void lowStorageUpdate(Oracle& o, const std::vector<double>* A, const std::vector
     }
 }
 
+/* Classic four-stage Runge-Kutta on the conserved variables. NO REFERENCE COUNTERPART:
+ * the reference's README.md:26 names "rk4", but src/ implements only the two RK3 schemes,
+ * so this is a restatement of the textbook method (Kutta 1901), not of reference code:
+ *   k1 = R(q0), q1 = q0 + dt/2 k1;  k2 = R(q1), q2 = q0 + dt/2 k2;
+ *   k3 = R(q2), q3 = q0 + dt k3;    k4 = R(q3), q  = q0 + dt/6 (k1 + 2 k2 + 2 k3 + k4),
+ * with the weighted sum accumulated as K = k1, K += 2 k2, K += 2 k3 as the stages arrive,
+ * and the velocities of each stage state recovered as momentum / rho (the RK3 schemes'
+ * deviceMul / deviceDiv convention, src/cuda_main.cu:127-139). */
+void rk4Step(Oracle& o) {
+    const long long N = (long long)o.N;
+    const double dt = o.dt;
+    std::vector<double> Q0[5], K[5];
+    for (int f = 0; f < 5; f++) { Q0[f].resize(N); K[f].resize(N); }
+#pragma omp parallel for schedule(static)
+    for (long long gl = 0; gl < N; gl++) {
+        Q0[0][gl] = o.r[gl];
+        Q0[1][gl] = o.r[gl] * o.u[gl]; Q0[2][gl] = o.r[gl] * o.v[gl]; Q0[3][gl] = o.r[gl] * o.w[gl];
+        Q0[4][gl] = o.e[gl];
+    }
+    auto set_state = [&](long long gl, const double* q) {
+        o.r[gl] = q[0]; o.e[gl] = q[4];
+        o.u[gl] = q[1] / q[0]; o.v[gl] = q[2] / q[0]; o.w[gl] = q[3] / q[0];
+    };
+    for (int st = 0; st < 4; st++) {
+        calcRHS(o, o.R1);
+#pragma omp parallel for schedule(static)
+        for (long long gl = 0; gl < N; gl++) {
+            double q[5];
+            for (int f = 0; f < 5; f++) {
+                const double k = o.R1[f][gl];
+                if (st == 0) { K[f][gl] = k; q[f] = Q0[f][gl] + 0.5 * dt * k; }
+                else if (st == 1) { K[f][gl] = K[f][gl] + 2.0 * k; q[f] = Q0[f][gl] + 0.5 * dt * k; }
+                else if (st == 2) { K[f][gl] = K[f][gl] + 2.0 * k; q[f] = Q0[f][gl] + dt * k; }
+                else q[f] = Q0[f][gl] + dt / 6.0 * (K[f][gl] + k);
+            }
+            set_state(gl, q);
+        }
+    }
+}
+
 int run(Oracle& o, int nsteps, double* par1, double* par2, double* timearr, double* dtlog, double* dpdzlog) {
     const long long N = (long long)o.N;
     for (int istep = 0; istep < nsteps; istep++) {
@@ -706,6 +747,8 @@ int run(Oracle& o, int nsteps, double* par1, double* par2, double* timearr, doub
             calcRHS(o, o.R1); lowStorageUpdate(o, o.R1, o.R1, 0);
             calcRHS(o, o.R2); lowStorageUpdate(o, o.R1, o.R2, 1);
             calcRHS(o, o.R1); lowStorageUpdate(o, o.R2, o.R1, 2);
+        } else if (o.p.scheme == CNS_RK4_CLASSIC) {
+            rk4Step(o);
         } else {
             /* runSimulation, src/cuda_main.cu:44-107 */
             const double dt = o.dt;

@@ -6,8 +6,8 @@ import numpy as np
 import pytest
 
 from cudanavierstokes_gb300.initial import tgv_fields
-from cudanavierstokes_gb300.params import (Derived, RK3_CLASSIC, boundary_layer_params, channel_params,
-                                           tgv_params)
+from cudanavierstokes_gb300.params import (Derived, RK3_CLASSIC, RK4_CLASSIC, boundary_layer_params,
+                                           channel_params, tgv_params)
 from tests._util import rel_err, smooth_random_state
 
 
@@ -115,6 +115,25 @@ def test_classic_rk3_third_order(oracle_mod):
     e1 = rel_err(res[0.4][1], res[0.05][1])
     e2 = rel_err(res[0.2][1], res[0.05][1])
     assert e1 / e2 > 6.0, (e1, e2)
+
+
+def test_classic_rk4_fourth_order(oracle_mod):
+    """The oracle's RK4 (a textbook restatement; the reference has no RK4): halving dt cuts
+    the time-integration error by ~16."""
+    base = tgv_params(16).copy(scheme=RK4_CLASSIC)
+    f = smooth_random_state(base, seed=6)
+    res = {}
+    T = None
+    for cfl in (0.4, 0.2, 0.05):
+        o = oracle_mod.Oracle(base.copy(cfl=cfl, check_cfl=10**6))
+        o.set_state(*f)
+        dt = o.calc_dt()
+        T = T or 8 * dt
+        o.run(int(round(T / dt)))
+        res[cfl] = o.get_state()
+    e1 = rel_err(res[0.4][1], res[0.05][1])
+    e2 = rel_err(res[0.2][1], res[0.05][1])
+    assert e1 / e2 > 12.0, (e1, e2)
 
 
 def test_tgv_kinetic_energy_decays(oracle_mod):

@@ -169,8 +169,6 @@ def test_run_parity(gpu_lib, oracle_mod, case):
         o, s = _bl_setup(oracle_mod, p)
     else:
         o, s = _pair(oracle_mod, p, f)
-    if case == "tgv_rk4":
-        pytest.skip("RK4 has no oracle counterpart (the reference has no RK4); covered by the order test")
     lo = o.run(n)
     lg = s.run(n)
     errs = state_errors(s.copy_field_out(), o.get_state())
