@@ -64,7 +64,32 @@ __global__ void __launch_bounds__(256) k_pow(const double* __restrict__ x, doubl
     }
 }
 
+__global__ void __launch_bounds__(256) k_rcp(const double* __restrict__ x, double* __restrict__ fast,
+                                             double* __restrict__ lib, long long n) {
+    for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x) {
+        fast[t] = cns::rcp_nr(x[t]);
+        lib[t] = 1.0 / x[t];
+    }
+}
+
 }  // namespace
+
+extern "C" int cns_selftest_rcp(int device, const double* x, long long n, double* fast, double* lib) {
+    if (!x || !fast || !lib || n < 1 || n > (1LL << 27)) return CNS_ERR_INVALID;
+    if (cudaSetDevice(device) != cudaSuccess) return CNS_ERR_CUDA;
+    double* buf = nullptr;
+    const size_t nb = (size_t)n;
+    if (cudaMalloc(&buf, nb * 3 * sizeof(double)) != cudaSuccess) return CNS_ERR_OOM;
+    cudaError_t e = cudaMemcpy(buf, x, nb * 8, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) {
+        k_rcp<<<1024, 256>>>(buf, buf + nb, buf + 2 * nb, n);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = cudaMemcpy(fast, buf + nb, nb * 8, cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess) e = cudaMemcpy(lib, buf + 2 * nb, nb * 8, cudaMemcpyDeviceToHost);
+    cudaFree(buf);
+    return e == cudaSuccess ? CNS_OK : CNS_ERR_CUDA;
+}
 
 extern "C" int cns_selftest_pow(int device, const double* x, long long n, double a, double* fast, double* lib) {
     if (!x || !fast || !lib || n < 1 || n > (1LL << 27)) return CNS_ERR_INVALID;

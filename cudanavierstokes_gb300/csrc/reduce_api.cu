@@ -10,6 +10,7 @@
 #include <cstdio>
 
 #include "../../include/cns.h"
+#include "cns_internal.h"
 
 namespace {
 
@@ -40,8 +41,11 @@ __global__ void __launch_bounds__(PLANE_THREADS) k_plane_reduce(int mx, int my, 
     const long long base = (long long)k * mx * my;
     const double dyinv = 1.0 / dy, dzinv = 1.0 / dz, vyz = dy * dz;
     double dtmin = 100000.0, sr = 0, srw = 0, se = 0, sk = 0;
-    for (int t = threadIdx.x; t < mx * my; t += blockDim.x) {
-        const int i = t % mx;
+    // 64-bit loop bound: the plane holds fewer than 2^31 points (checked on the host), so
+    // t + blockDim.x cannot overflow
+    const long long n = (long long)mx * my;
+    for (long long t = threadIdx.x; t < n; t += blockDim.x) {
+        const int i = (int)(t % mx);
         const long long c = base + t;
         const double rr = r[c], uu = u[c], vv = v[c], ww = w[c], ee = e[c];
         const double ien = ee / rr - 0.5 * (uu * uu + vv * vv + ww * ww);
@@ -89,15 +93,32 @@ __global__ void __launch_bounds__(32) k_plane_final(int mz, const double* __rest
     out[0] = a; out[1] = b; out[2] = c; out[3] = d; out[4] = f;
 }
 
-int check_args(int mx, int my, int mz, const void* const* ptrs, int n, double dy, double dz, double gam, double cfl) {
-    if (mx < 1 || my < 1 || mz < 1 || (long long)mx * my > (1LL << 31)) return CNS_ERR_INVALID;
+}  // namespace
+
+namespace cns {
+// Argument check shared by the reduction entry points: a plane of fewer than 2^31 points,
+// non-null pointers, positive spacings, gam > 1, cfl > 0. Records the message under `who`.
+int check_reduce_args(const char* who, int mx, int my, int mz, const void* const* ptrs, int n, double dy, double dz,
+                      double gam, double cfl) {
+    char buf[200];
+    if (mx < 1 || my < 1 || mz < 1 || (long long)mx * my >= (1LL << 31)) {
+        snprintf(buf, sizeof buf, "%s: grid %d x %d x %d (every edge >= 1, mx*my < 2^31)", who, mx, my, mz);
+        return set_error(CNS_ERR_INVALID, buf);
+    }
+    static const char* names[] = {"r", "u", "v", "w", "e", "mu", "dxv", "out"};
     for (int q = 0; q < n; q++)
-        if (!ptrs[q]) return CNS_ERR_INVALID;
-    if (!(dy > 0) || !(dz > 0) || !(gam > 1) || !(cfl > 0)) return CNS_ERR_INVALID;
+        if (!ptrs[q]) {
+            snprintf(buf, sizeof buf, "%s: %s is NULL", who, q < 8 ? names[q] : "pointer");
+            return set_error(CNS_ERR_INVALID, buf);
+        }
+    if (!(dy > 0) || !(dz > 0) || !(gam > 1) || !(cfl > 0)) {
+        snprintf(buf, sizeof buf, "%s: dy = %g, dz = %g, gam = %g, cfl = %g (need dy, dz, cfl > 0, gam > 1)", who,
+                 dy, dz, gam, cfl);
+        return set_error(CNS_ERR_INVALID, buf);
+    }
     return CNS_OK;
 }
-
-}  // namespace
+}  // namespace cns
 
 namespace cns {
 // launch the two reduction passes with the given scratch (5*mz doubles)
@@ -113,16 +134,25 @@ int launch_plane_reduce(int mx, int my, int mz, const double* r, const double* u
 extern "C" int cns_reduce_state(int mx, int my, int mz, const double* r, const double* u, const double* v,
                                 const double* w, const double* e, const double* mu, const double* dxv, double dy,
                                 double dz, double gam, double cfl, double* out, void* stream) {
-    const void* ptrs[9] = {r, u, v, w, e, mu, dxv, out, (const void*)1};
-    if (check_args(mx, my, mz, ptrs, 8, dy, dz, gam, cfl)) return CNS_ERR_INVALID;
+    const void* ptrs[8] = {r, u, v, w, e, mu, dxv, out};
+    if (int rc = cns::check_reduce_args("cns_reduce_state", mx, my, mz, ptrs, 8, dy, dz, gam, cfl)) return rc;
     cudaStream_t s = (cudaStream_t)stream;
     double* scratch = nullptr;
-    if (cudaMalloc(&scratch, 5 * (size_t)mz * sizeof(double)) != cudaSuccess) {
+    const size_t bytes = 5 * (size_t)mz * sizeof(double);
+    if (cudaError_t ce = cudaMalloc(&scratch, bytes); ce != cudaSuccess) {
         cudaGetLastError();
-        return CNS_ERR_OOM;
+        char buf[200];
+        snprintf(buf, sizeof buf, "cns_reduce_state: cudaMalloc of %zu bytes of plane partials failed: %s", bytes,
+                 cudaGetErrorString(ce));
+        return cns::set_error(CNS_ERR_OOM, buf);
     }
     int rc = cns::launch_plane_reduce(mx, my, mz, r, u, v, w, e, mu, dxv, dy, dz, gam, cfl, scratch, out, s);
-    if (cudaStreamSynchronize(s) != cudaSuccess) rc = CNS_ERR_CUDA;
+    if (rc) cns::set_error(rc, "cns_reduce_state: kernel launch failed");
+    if (cudaError_t ce = cudaStreamSynchronize(s); ce != cudaSuccess) {
+        char buf[200];
+        snprintf(buf, sizeof buf, "cns_reduce_state: %s", cudaGetErrorString(ce));
+        rc = cns::set_error(CNS_ERR_CUDA, buf);
+    }
     cudaFree(scratch);
     return rc;
 }

@@ -1,11 +1,11 @@
 // reduce_noalloc.cu -- cns_reduce_state_noalloc: the CFL time step and volume integrals
 // of cns_reduce_state for callers that cannot allocate device memory.
 //
-// Who needs it: code that issues work while a CUDA stream is being captured into a graph
-// (cudaMalloc/cudaFree are not allowed inside a capture, and cudaFree synchronises the
-// device), code running under an external memory manager that owns every device
-// allocation (a framework's caching allocator or a fixed HBM budget), and real-time loops
-// that must not block on the allocator. They pass their own input and output buffers; the
+// Who needs it: code running under a memory manager that owns every device allocation
+// of the process (a host framework's caching allocator, or a solver service that divides
+// a fixed HBM budget among its simulations and may not let a library take memory behind
+// its back), and time-critical loops that must not call cudaMalloc/cudaFree, whose
+// cudaFree waits for the whole device. They pass their own input and output buffers; the
 // per-plane partial sums live in a fixed file-scope device array instead of a cudaMalloc'd
 // scratch buffer.
 //
@@ -39,7 +39,9 @@ double* g_scratch_addr[MAX_DEVICES] = {};
 
 // Device address of the scratch array on the current device. In host code the symbol
 // g_plane_scratch is only a host-side stand-in, so the address is queried once per device
-// with that device current and cached.
+// with that device current and cached: the first call on a device does this set-up. The
+// cached address belongs to the device's primary context; after cudaDeviceReset on that
+// device the address is stale and later calls are invalid.
 int scratch_address(double** out) {
     int dev = -1;
     if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= MAX_DEVICES) {
@@ -74,9 +76,8 @@ extern "C" int cns_reduce_state_noalloc(int mx, int my, int mz, const double* r,
                  CNS_NOALLOC_MAX_PLANES);
         return cns::set_error(CNS_ERR_INVALID, buf);
     }
-    if (mx < 1 || my < 1 || mz < 1 || (long long)mx * my > (1LL << 31) || !r || !u || !v || !w || !e || !mu || !dxv ||
-        !out || !(dy > 0) || !(dz > 0) || !(gam > 1) || !(cfl > 0))
-        return cns::set_error(CNS_ERR_INVALID, "cns_reduce_state_noalloc: invalid argument");
+    const void* ptrs[8] = {r, u, v, w, e, mu, dxv, out};
+    if (int bad = cns::check_reduce_args("cns_reduce_state_noalloc", mx, my, mz, ptrs, 8, dy, dz, gam, cfl)) return bad;
     double* scratch = nullptr;
     int rc = scratch_address(&scratch);
     if (rc) return rc;

@@ -160,7 +160,11 @@ void cns_server::loop() {
             if (st >= r->nsteps) finish(this, r);
             else still.push_back(r);
         }
-        running.swap(still);
+        {
+            // every change of `running` holds the lock: cns_server_stats reads its size
+            std::lock_guard<std::mutex> lk(mu);
+            running.swap(still);
+        }
         cv_done.notify_all();
     }
 }

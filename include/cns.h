@@ -238,16 +238,19 @@ CNS_API int cns_reduce_state(int mx, int my, int mz, const double* r, const doub
                              double dz, double gam, double cfl, double* out, void* stream);
 
 /* Allocation-free variant of cns_reduce_state; it has no counterpart in the reference.
- * For callers that may not call cudaMalloc: work issued while a stream is captured into
- * a CUDA graph, code whose device memory belongs to another allocator or a fixed HBM
- * budget, and loops that must not block on allocation. Same arguments and results as
- * cns_reduce_state, but the per-plane partials live in a fixed device array of
- * 5 * CNS_NOALLOC_MAX_PLANES doubles (160 KiB, held by every GPU that loads the library)
- * and the call neither allocates nor frees memory nor synchronises: results are ready
- * when `stream` reaches this point. mz > CNS_NOALLOC_MAX_PLANES is rejected with
- * CNS_ERR_INVALID. The first call on a device looks up the array's device address (a
- * one-time cudaGetSymbolAddress with that device current); make that first call before
- * any stream capture. All calls share the array: calls whose work overlaps on the GPU
+ * For callers that may not call cudaMalloc: code whose device memory all belongs to
+ * another allocator (a host framework's caching allocator) or to a fixed HBM budget
+ * that a serving process divides among its simulations, and time-critical loops that
+ * must not block in cudaMalloc/cudaFree (cudaFree waits for the whole device). Same
+ * arguments and results as cns_reduce_state, but the per-plane partials live in a fixed
+ * device array of 5 * CNS_NOALLOC_MAX_PLANES doubles (160 KiB, held by every GPU that
+ * loads the library until the process exits) and the call neither allocates nor frees
+ * memory nor synchronises: results are ready when `stream` reaches this point.
+ * mz > CNS_NOALLOC_MAX_PLANES is rejected with CNS_ERR_INVALID. The first call on a
+ * device looks up the array's device address (a one-time cudaGetSymbolAddress with that
+ * device current); make that first call before any stream capture. After
+ * cudaDeviceReset on a device the looked-up address is stale and later calls on that
+ * device are invalid. All calls share the array: calls whose work overlaps on the GPU
  * race and must be serialised by the caller. */
 #define CNS_NOALLOC_MAX_PLANES 4096
 CNS_API int cns_reduce_state_noalloc(int mx, int my, int mz, const double* r, const double* u, const double* v,
@@ -367,6 +370,11 @@ CNS_API int cns_selftest_convert(int device, const double* x, const float* y, lo
  * viscosity law (T^viscexp) next to the CUDA library pow on the same n <= 2^27 host
  * values. */
 CNS_API int cns_selftest_pow(int device, const double* x, long long n, double a, double* fast, double* lib);
+
+/* Self test with no counterpart in the reference: the solver's FP64 reciprocal (an FP32
+ * seed and two Newton steps, used for 1/rho in every stage update and state recovery)
+ * next to the IEEE division 1.0 / x on the same n <= 2^27 host values. */
+CNS_API int cns_selftest_rcp(int device, const double* x, long long n, double* fast, double* lib);
 
 #ifdef __cplusplus
 }

@@ -1,8 +1,8 @@
 """The allocation-free reduction entry point against the allocating one, through the C ABI.
 
-cns_reduce_state_noalloc serves callers that may not allocate device memory (stream
-capture, externally managed memory, allocation-free loops): its partial sums live in a
-fixed device array shared by every call. This file is collected last so that a run which
+cns_reduce_state_noalloc serves callers that may not allocate device memory (memory owned
+by another allocator or a fixed budget, loops that must not block in the allocator): its
+partial sums live in a fixed device array shared by every call. This file is collected last so that a run which
 stops at the first failure has run every other test before it; it also passes on its own
 in a fresh process (the array's device address is looked up on the first call).
 """
