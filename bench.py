@@ -14,13 +14,14 @@ path is not sharded across GPUs, each rank advances its own channel).
   roofline    the RHS + stage-update kernel (dominant kernel): its event-timed average
               launch against the FP64 pipe (measured live) and against HBM
   cpu_baseline  the CPU oracle (the reference's algorithm restated, OpenMP) on the host
-              cores, on a z-slab of the same channel
+              cores, on the same full channel (whole RK3 steps for ~12 s)
   fp32_rhs    the same workload with the RHS in FP32 (state/accumulation FP64)
   batched     48 Taylor-Green boxes of uneven size (seeded), FP32 RHS / FP64 state, one
               persistent launch per RK stage for the whole ensemble, graph replay, autotuned
   serving     Poisson-arrival "advance N steps" requests (Taylor-Green 32^3-192^3 and
               64x48x64 channels, N in [50, 500]) under a 150 GB budget: p50/p99 latency and
-              aggregate Mpoint-steps/s per arrival rate
+              aggregate Mpoint-steps/s per arrival rate, 100 requests per rate, rates swept
+              from light load to past the batch's capacity
 
 --impl reference times the CPU port of the reference's path (the reference itself only
 has a GPU path) on all host cores, on the same workload and metric.
@@ -46,7 +47,6 @@ METRIC = "Mpoint-steps/s"
 PEAKS_FILE = os.path.join(REPO, "MEASURED_PEAKS.json")
 TRAFFIC_FILE = os.path.join(REPO, "profiles", "rhs_kernel_channel_traffic.txt")
 TRAFFIC_FILE_FP32 = os.path.join(REPO, "profiles", "rhs_kernel_channel_fp32_traffic.txt")
-SLAB_MZ = 24   # CPU sample: full x-y cross-section, 24 streamwise planes
 
 
 def parse_args():
@@ -64,8 +64,8 @@ def parse_args():
     ap.add_argument("--precision", choices=["fp64", "fp32"], default="fp64")
     ap.add_argument("--no-extras", action="store_true", help="skip fp32/cpu/e2e side measurements")
     ap.add_argument("--grid", default=None, help="override the grid as MX,MY,MZ (profiling of smaller cases)")
-    ap.add_argument("--serve-requests", type=int, default=16, help="requests per arrival rate in the serving leg")
-    ap.add_argument("--serve-rates", default="1.0,3.0", help="arrival rates (requests/s) of the serving leg")
+    ap.add_argument("--serve-requests", type=int, default=100, help="requests per arrival rate in the serving leg")
+    ap.add_argument("--serve-rates", default="2,4,8,16", help="arrival rates (requests/s) of the serving leg")
     return ap.parse_args()
 
 
@@ -182,9 +182,11 @@ def barrier(world: int):
 
 
 def cpu_sample(p, steps_min: int = 2, seconds: float = 12.0):
-    """Time the CPU oracle on a z-slab of the workload: returns Mpoint-steps/s, threads, text."""
+    """Time the CPU oracle on the full workload grid on all host cores, whole RK3 steps until
+    `seconds` have passed: returns Mpoint-steps/s, threads, text."""
     from oracle import oracle as orc
-    q = p.copy(mz=SLAB_MZ, Lz=p.Lz * SLAB_MZ / p.mz, precision=0)
+    q = p.copy(precision=0)
+    orc.set_threads(os.cpu_count() or 1)
     o = orc.Oracle(q)
     o.set_state(*initial_state(q, o.grid()["x"]))
     o.run(1)                       # warm-up step
@@ -194,8 +196,8 @@ def cpu_sample(p, steps_min: int = 2, seconds: float = 12.0):
         n += 1
     dt = time.perf_counter() - t0
     pts = q.npoints
-    return pts * n / dt / 1e6, orc.max_threads(), (f"{n} RK3 steps of a {q.mx}x{q.my}x{q.mz} z-slab of the workload "
-                                                    f"({pts} points, same physics and stencils), {dt:.1f} s")
+    return pts * n / dt / 1e6, orc.max_threads(), (f"{n} RK3 steps of the full {q.mx}x{q.my}x{q.mz} workload grid "
+                                                    f"({pts} points, FP64, same physics and stencils), {dt:.1f} s")
 
 
 def run_batched(args, stream_ptr, members=48, mode_req="tuned", with_other=True):
@@ -259,15 +261,24 @@ def run_batched(args, stream_ptr, members=48, mode_req="tuned", with_other=True)
 
 
 def run_serving(args):
-    """BASELINE config 4: Poisson arrivals of advance-N-steps requests, continuous batching."""
+    """BASELINE config 4: Poisson arrivals of advance-N-steps requests, continuous batching.
+    The requests' initial fields are generated once per (kind, grid) before the clock starts
+    and shared by the requests of that grid (the work of a request does not depend on its
+    field values: N steps of its grid)."""
     import threading
     from cudanavierstokes_gb300.server import Server
     from cudanavierstokes_gb300.workloads import request_fields, serving_requests
     rates = [float(r) for r in args.serve_rates.split(",") if r]
     res = []
+    pool = {}
     for rate in rates:
         reqs = serving_requests(args.serve_requests, rate, seed=1)
-        fields = [request_fields(p, kind, sd) for (_, p, kind, _, sd) in reqs]   # prepared before the clock starts
+        fields = []
+        for (_, p, kind, _, sd) in reqs:
+            key = (kind, p.mx, p.my, p.mz)
+            if key not in pool:
+                pool[key] = [np.ascontiguousarray(a) for a in request_fields(p, kind, sd)]
+            fields.append(pool[key])
         srv = Server(precision=1, hbm_budget_bytes=150 * 10**9)
         ids = []
         t0 = time.perf_counter()
@@ -286,12 +297,14 @@ def run_serving(args):
         wall = time.perf_counter() - t0
         st = srv.stats()
         srv.close()
+        offered = sum(p.npoints * n for (_, p, _, n, _) in reqs) / reqs[-1][0] / 1e6
         res.append({"rate_per_s": rate, "requests": len(reqs), "p50_s": st["p50_s"], "p99_s": st["p99_s"],
                     "max_s": st["max_s"], "value": st["point_steps"] / wall / 1e6, "unit": "Mpoint-steps/s",
-                    "busy_value": st["point_steps"] / max(st["busy_seconds"], 1e-9) / 1e6,
+                    "offered": offered, "busy_value": st["point_steps"] / max(st["busy_seconds"], 1e-9) / 1e6,
                     "batch_steps": st["batch_steps"], "wall_s": wall})
     return {"rates": res, "workload": "Poisson arrivals, N ~ U[50,500] steps, Taylor-Green 32^3-192^3 (Re, Ma as "
-                                      "the ensemble) and 64x48x64 channels (25 %), FP32 RHS, 150 GB HBM budget"}
+                                      "the ensemble) and 64x48x64 channels (25 %), FP32 RHS, 150 GB HBM budget; "
+                                      "'offered' = the requests' point-steps / their arrival span"}
 
 
 def ke_series(p, fields, t_end, chunk=250):
@@ -388,31 +401,63 @@ def read_traffic(N: int, fp32: bool = False):
 
 
 def run_reference(args, world, rank):
-    """CPU port of the reference path (the oracle) on all host cores, rank 0 only."""
+    """CPU port of the reference path (the oracle) on all host cores, rank 0 only, on the
+    full workload grid: W untimed steps, then K timed steps."""
     if rank != 0:
         return
     from oracle import oracle as orc
     p, desc = workload(args.workload, "fp64", args.grid)
-    q = p.copy(mz=SLAB_MZ, Lz=p.Lz * SLAB_MZ / p.mz)
     orc.set_threads(os.cpu_count() or 1)
-    o = orc.Oracle(q)
-    o.set_state(*initial_state(q, o.grid()["x"]))
+    o = orc.Oracle(p)
+    o.set_state(*initial_state(p, o.grid()["x"]))
     for _ in range(args.warmup):
         o.run(1)
     t0 = time.perf_counter()
     o.run(args.steps)
     dt = time.perf_counter() - t0
-    v = q.npoints * args.steps / dt / 1e6
+    v = p.npoints * args.steps / dt / 1e6
     cores = orc.max_threads()
-    sample = (f"{args.steps} RK3 steps per timed region on a {q.mx}x{q.my}x{q.mz} z-slab of the workload "
-              f"({q.npoints} points, same physics/stencils), CPU restatement of the reference kernels (OpenMP)")
+    sample = (f"{args.steps} RK3 steps of the full {p.mx}x{p.my}x{p.mz} workload grid ({p.npoints} points, FP64) "
+              f"per timed region, CPU restatement of the reference kernels (OpenMP, {cores} threads)")
     line = {"impl": "reference", "metric": METRIC, "value": v, "unit": "Mpoint-steps/s", "n_gpus": args.gpus,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": dt / args.steps * 1e3 * p.npoints / q.npoints,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": dt / args.steps * 1e3,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": {"workload": desc, "grid": [p.mx, p.my, p.mz], "points": p.npoints},
+            "config": {"workload": desc, "grid": [p.mx, p.my, p.mz], "points": p.npoints, "precision": "fp64",
+                       "parallelism": "replicas x1"},
             "cpu_baseline": {"value": v, "unit": "Mpoint-steps/s", "cores": cores, "kind": "port", "sample": sample},
             "e2e": {"value": v, "unit": "Mpoint-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
+
+
+def hbm_peak_gbs():
+    try:
+        with open(PEAKS_FILE) as f:
+            return float(json.load(f)["hbm_gbs"]), "measured (MEASURED_PEAKS.json, of measured)"
+    except Exception:
+        return 6800.0, "fallback (of fallback)"
+
+
+def fp32_roofline(N, S, V, ph, fp32_peak):
+    """Roofline object of the FP32-RHS RHS + stage kernel: algorithmic bytes (FP64 state and
+    FP32 RK register in and out, 160 B/point) against the measured HBM bandwidth, with the
+    FP32 algorithmic flops against the live FP32 FMA peak and the ncu DRAM traffic beside."""
+    from cudanavierstokes_gb300 import roofline as rf
+    rhs_s = ph["rhs_ms"] * 1e-3
+    hbm_peak, hbm_src = hbm_peak_gbs()
+    ach = rf.RHS_KERNEL_BYTES * N / rhs_s / 1e9
+    tf = rf.fused_rhs_kernel_flops(S, V) * N / rhs_s / 1e12
+    kv = read_profile_summary(TRAFFIC_FILE_FP32)
+    out = {"bound": "hbm", "kernel": "k_rhs<float> (FP32 RHS x/y/z + body force + sponge + FP64 RK stage update + "
+           "next-stage state recovery)", "achieved": ach, "peak": hbm_peak, "unit": "GB/s", "frac": ach / hbm_peak,
+           "peak_source": hbm_src, "traffic": read_traffic(N, fp32=True), "launch_ms": ph["rhs_ms"],
+           "bytes_per_point": rf.RHS_KERNEL_BYTES, "flops_per_point": rf.fused_rhs_kernel_flops(S, V),
+           "fp32": {"achieved": tf, "peak": fp32_peak, "unit": "TFLOP/s", "frac": tf / fp32_peak,
+                    "peak_source": "measured live (FMA-chain probe, cns_probe_fma_peak)"},
+           "phase_ms": ph}
+    if "fp64_inst_per_point" in kv:
+        out["executed"] = {k: float(v) for k, v in kv.items() if k.endswith(("_per_point", "_pct"))}
+        out["executed"]["source"] = "ncu --set full, profiles/rhs_kernel_channel_fp32.md"
+    return out
 
 
 def run_gb300(args, world, rank, local):
@@ -458,12 +503,7 @@ def run_gb300(args, world, rank, local):
     native.check(native.lib().cns_probe_fma_peak(local, 1 if args.precision == "fp64" else 0,
                                                  2000 if args.precision == "fp64" else 20000,
                                                  native.ctypes.byref(t64)))
-    try:
-        with open(PEAKS_FILE) as f:
-            hbm_peak = float(json.load(f)["hbm_gbs"])
-        hbm_src = "measured (MEASURED_PEAKS.json)"
-    except Exception:
-        hbm_peak, hbm_src = 6800.0, "fallback"
+    hbm_peak, hbm_src = hbm_peak_gbs()
     traffic = read_traffic(N, fp32=args.precision == "fp32")
     roof = {"bound": "fp64" if args.precision == "fp64" else "fp32", "kernel": "k_rhs (RHS x/y/z + body force + "
             "sponge + RK stage update)", "achieved": ach_tf, "peak": t64.value, "unit": "TFLOP/s",
@@ -474,6 +514,8 @@ def run_gb300(args, world, rank, local):
                     "peak_source": hbm_src},
             "phase_ms": ph}
     kv = read_profile_summary()
+    if args.precision == "fp32":
+        roof = fp32_roofline(N, S, V, ph, t64.value)
     if args.precision == "fp64" and "fp64_inst_per_point" in kv:
         # the algorithmic count above is the reference's operation structure; the kernel
         # executes fewer FP64 instructions (shared flux products, lambda/mu), so the
@@ -526,9 +568,12 @@ def run_gb300(args, world, rank, local):
             torch.cuda.synchronize()
             ms32 = e0.elapsed_time(e1)
             ph32 = s32.time_phases(6)
+            t32 = native.ctypes.c_double()
+            native.check(native.lib().cns_probe_fma_peak(local, 0, 20000, native.ctypes.byref(t32)))
             line["fp32_rhs"] = {"value": N * args.steps / (ms32 * 1e-3) / 1e6, "unit": "Mpoint-steps/s",
                                 "ms_per_step": ms32 / args.steps, "phase_ms": ph32,
-                                "speedup_vs_fp64": (ms / ms32)}
+                                "speedup_vs_fp64": (ms / ms32),
+                                "roofline": fp32_roofline(N, S, V, ph32, t32.value)}
             s32.close()
         # batched ensemble and serving (FP32 RHS / FP64 state)
         line["batched"] = run_batched(args, stream.cuda_stream)

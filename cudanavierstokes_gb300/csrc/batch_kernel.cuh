@@ -154,13 +154,13 @@ __global__ void __launch_bounds__(BATCH_THREADS, sizeof(R) == 4 ? 5 : 4)
         if (t < ghost_count(I.g)) {
             const RhsIn<R>& in = I.in[cur];
             const StencilFields<R> f{(R*)in.r, (R*)in.u, (R*)in.v, (R*)in.w, (R*)in.t, (R*)in.p, (R*)in.h,
-                                     (R*)in.m};
+                                     (R*)in.m, (float4*)in.qa, (float4*)in.qb};
             ghost_state_cell<R>(I.g, I.ph, f, I.scal, (int)t);
         }
     }
     grid_barrier(bar, nb, err);
-    // phase 2: dilatation (FP32-RHS: the RHS forms the nine gradients itself) or the nine
-    // velocity gradients and the dilatation
+    // phase 2: dilatation from the packed records (FP32-RHS: the RHS forms the nine gradients
+    // itself) or the nine velocity gradients and the dilatation
     for (long long u = blockIdx.x; u < npu; u += gridDim.x) {
         const int q = find_inst(ctl->unit_off, n, u);
         const BatchInst<R>& I = tab[q];
@@ -168,10 +168,14 @@ __global__ void __launch_bounds__(BATCH_THREADS, sizeof(R) == 4 ? 5 : 4)
         unit_point(I, u - ctl->unit_off[q], tx, ty, i, j, k);
         if (i < I.g.mx && j < I.g.my) {
             const RhsIn<R>& in = I.in[cur];
-            GradOut<R> go;
-            for (int c = 0; c < 9; c++) go.g[c] = (R*)in.g[c];
-            go.dil = (R*)in.dil;
-            grad_point<R, V, sizeof(R) == 4>(I.g, I.cf, in.u, in.v, in.w, go, i, j, k);
+            if constexpr (sizeof(R) == 4) {
+                dil_point_packed<V>(I.g, I.cf, in.qa, (float*)in.dil, i, j, k);
+            } else {
+                GradOut<R> go;
+                for (int c = 0; c < 9; c++) go.g[c] = (R*)in.g[c];
+                go.dil = (R*)in.dil;
+                grad_point<R, V>(I.g, I.cf, in.u, in.v, in.w, go, i, j, k);
+            }
         }
     }
     grid_barrier(bar, nb, err);

@@ -18,17 +18,23 @@ struct StateOut {
 
 // lambda = mu / (Pr Ec) at every point, ghosts included (wall and extrapolated ghosts
 // are formed from the same T or linearly), so only mu is stored and the RHS applies
-// the ratio once per point
+// the ratio once per point.
+//
+// FP64 mode: the stencil inputs rho, u, v, w are the state fields themselves and T, p, H,
+// mu are four FP64 fields (h, t, p, m). FP32-RHS mode: the eight stencil inputs are packed
+// per point into two 16-byte records, qa = (rho, u, v, w) and qb = (T, p, H, mu), so a
+// neighbour costs two vector loads (and one address each) instead of eight scalar loads.
 template <typename R>
 struct DerivedOut {
-    R *h, *t, *p, *m;
-    R *r32, *u32, *v32, *w32;   // FP32-RHS stencil copies (nullptr in FP64 mode)
+    R *h, *t, *p, *m;   // FP64 mode
+    float4 *qa, *qb;    // FP32-RHS mode
 };
 
 // the eight ghosted stencil inputs
 template <typename R>
 struct StencilFields {
-    R *r, *u, *v, *w, *t, *p, *h, *m;
+    R *r, *u, *v, *w, *t, *p, *h, *m;   // FP64 mode
+    float4 *qa, *qb;                    // FP32-RHS mode (packed, see DerivedOut)
 };
 
 template <typename R>
@@ -37,11 +43,13 @@ struct GradOut {
     R* dil;
 };
 
-// RHS stage kernel inputs
+// RHS stage kernel inputs (FP64: separate fields and the nine velocity gradients; FP32-RHS:
+// the packed records qa, qb and theta, the RHS kernel forms the gradients itself)
 template <typename R>
 struct RhsIn {
     const R *r, *u, *v, *w, *t, *p, *h, *m, *dil;
     const R* g[9];
+    const float4 *qa, *qb;
 };
 
 // time-scheme stage kinds
@@ -87,9 +95,13 @@ void launch_ghost_scalar(const Geom& g, R* f, cudaStream_t s);
 template <typename R>
 void launch_grad(int V, const Geom& g, const CoefT<R>& cf, const R* u, const R* v, const R* w, const GradOut<R>& o,
                  int own, cudaStream_t s);
+// FP32-RHS dilatation (and its ghost images with own) from the packed records (rho, u, v, w)
+void launch_dil_packed(int V, const Geom& g, const CoefT<float>& cf, const float4* qa, float* dil, int own,
+                       cudaStream_t s);
+// mu[c * mstride]: 1 for an FP64 field, 4 for the mu slot of the packed FP32 records
 template <typename R>
-int launch_reduce(const Geom& g, const Phys& ph, const StateIn& q, const R* mu, double* part, int want, double* scal,
-                  double* diag, cudaStream_t s);
+int launch_reduce(const Geom& g, const Phys& ph, const StateIn& q, const R* mu, int mstride, double* part, int want,
+                  double* scal, double* diag, cudaStream_t s);
 template <typename T>
 void launch_unpack(const Geom& g, const double* src, T* dst, cudaStream_t s);
 template <typename T>
@@ -97,6 +109,10 @@ void launch_pack(const Geom& g, const T* src, double* dst, cudaStream_t s);
 
 // record `msg` as the calling thread's cns_last_error() text and return `code`
 int set_error(int code, const char* msg);
+
+// argument check of the stateless reductions (records the message under `who`)
+int check_reduce_args(const char* who, int mx, int my, int mz, const void* const* ptrs, int n, double dy, double dz,
+                      double gam, double cfl);
 
 // the RHS + stage kernel over the interior; returns the number of launches (band groups)
 int launch_rhs_fp64(int S, int V, const Geom& g, const Phys& ph, const CoefT<double>& cf, const RhsIn<double>& in,

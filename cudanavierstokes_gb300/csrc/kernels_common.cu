@@ -38,69 +38,14 @@ __global__ void __launch_bounds__(128) k_grad(Geom g, CoefT<R> cf, const R* __re
     grad_point<R, V, sizeof(R) == 4>(g, cf, u, v, w, o, i, j, (int)blockIdx.z, own != 0);
 }
 
-// FP32-RHS dilatation for two neighbouring x points per thread (i even, i + 1): each
-// neighbour load is one aligned 8-byte pair, the x stencil of the pair comes from V + 1 such
-// pairs; per point the arithmetic is grad_point's (DIL_ONLY), so the values are the same.
-// When mx is odd the last pair's second point is the first ghost cell: it is computed from
-// padding values inside the allocation and not stored.
+// FP32-RHS dilatation from the packed records (rho, u, v, w), one point per thread
 template <int V>
-__global__ void __launch_bounds__(128) k_dil_pair(Geom g, CoefT<float> cf, const float* __restrict__ u,
-                                                  const float* __restrict__ v, const float* __restrict__ w,
-                                                  float* __restrict__ dil, int own) {
-    const int i = 2 * (int)(blockIdx.x * blockDim.x + threadIdx.x);
+__global__ void __launch_bounds__(128) k_dil_packed(Geom g, CoefT<float> cf, const float4* __restrict__ qa,
+                                                    float* __restrict__ dil, int own) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
     const int j = blockIdx.y * blockDim.y + threadIdx.y;
     if (i >= g.mx || j >= g.my) return;
-    const int k = (int)blockIdx.z;
-    const int c = (int)g.at(i, j, k);   // even: rows and planes are padded to multiples of 16
-    const auto ld2 = [](const float* p, int o) { return __ldg(reinterpret_cast<const float2*>(p + o)); };
-    // x: u at i - V .. i + 1 + V from the pairs at even offsets -V - (V & 1) .. V + 1
-    float ux[2 * V + 4];
-#pragma unroll
-    for (int o = -V - (V & 1); o <= V + 1; o += 2) {
-        const float2 pr = ld2(u, c + o);
-        ux[o + V + 1] = pr.x;
-        ux[o + V + 2] = pr.y;
-    }
-    float th[2];
-#pragma unroll
-    for (int l = 0; l < 2; l++) {   // the pair's two points
-        const auto at = [&](int off) { return ux[l + off + V + 1]; };
-        float s = cf.c1V[0][1] * (at(1) - at(-1));
-#pragma unroll
-        for (int kk = 2; kk <= V; kk++) s = fma(cf.c1V[0][kk], at(kk) - at(-kk), s);
-        if (g.nonuniform_x) s *= cf.xp[min(i + l, g.mx - 1)];
-        th[l] = s;
-    }
-    float2 dy, dz;
-    {
-        const int P = (int)g.P, PS = (int)g.PS;
-        float2 a = ld2(v, c + P), b = ld2(v, c - P);
-        float sy0 = cf.c1V[1][1] * (a.x - b.x), sy1 = cf.c1V[1][1] * (a.y - b.y);
-        a = ld2(w, c + PS); b = ld2(w, c - PS);
-        float sz0 = cf.c1V[2][1] * (a.x - b.x), sz1 = cf.c1V[2][1] * (a.y - b.y);
-#pragma unroll
-        for (int kk = 2; kk <= V; kk++) {
-            a = ld2(v, c + kk * P); b = ld2(v, c - kk * P);
-            sy0 = fma(cf.c1V[1][kk], a.x - b.x, sy0);
-            sy1 = fma(cf.c1V[1][kk], a.y - b.y, sy1);
-            a = ld2(w, c + kk * PS); b = ld2(w, c - kk * PS);
-            sz0 = fma(cf.c1V[2][kk], a.x - b.x, sz0);
-            sz1 = fma(cf.c1V[2][kk], a.y - b.y, sz1);
-        }
-        dy = make_float2(sy0, sy1);
-        dz = make_float2(sz0, sz1);
-    }
-    const float t0 = th[0] + dy.x + dz.x, t1 = th[1] + dy.y + dz.y;
-    if (i + 1 < g.mx) {
-        *reinterpret_cast<float2*>(dil + c) = make_float2(t0, t1);
-        if (own) {
-            dil_ghost_owner<float>(g, dil, c, i, j, k, t0);
-            dil_ghost_owner<float>(g, dil, c + 1, i + 1, j, k, t1);
-        }
-    } else {
-        dil[c] = t0;
-        if (own) dil_ghost_owner<float>(g, dil, c, i, j, k, t0);
-    }
+    dil_point_packed<V>(g, cf, qa, dil, i, j, (int)blockIdx.z, own != 0);
 }
 
 template <typename R>
@@ -130,7 +75,7 @@ __device__ __forceinline__ double warp_min(double v) {
 
 template <typename R>
 __global__ void __launch_bounds__(RED_THREADS) k_reduce_partial(Geom g, Phys ph, StateIn q, const R* __restrict__ mu,
-                                                                double* part, int want) {
+                                                                int mstride, double* part, int want) {
     __shared__ double sh[6][RED_THREADS / 32];
     const long long n = (long long)g.mx * g.my * g.mz;
     double dtmin = 100000.0, s_r = 0.0, s_rw = 0.0, s_e = 0.0, s_k = 0.0, s_rk = 0.0;
@@ -149,7 +94,7 @@ __global__ void __launch_bounds__(RED_THREADS) k_reduce_partial(Geom g, Phys ph,
             double sos = sqrt(ph.gam * (ph.gam - 1) * ien);
             double dx = g.dxv[i];
             double d2x = dx * dx;
-            double m = to_d<R>(mu[c]);
+            double m = to_d<R>(mu[c * mstride]);
             double ci = fmax((fabs(uu) + sos) / dx, fmax((fabs(vv) + sos) * g.dy, (fabs(ww) + sos) * g.dz));
             double vi = fmax(m / d2x, fmax(m * g.d2y, m * g.d2z));
             dtmin = fmin(dtmin, ph.cfl / fmax(ci, vi));
@@ -269,30 +214,29 @@ void launch_ghost_scalar(const Geom& g, R* f, cudaStream_t s) {
 template <typename R>
 void launch_grad(int V, const Geom& g, const CoefT<R>& cf, const R* u, const R* v, const R* w, const GradOut<R>& o,
                  int own, cudaStream_t s) {
-    if constexpr (sizeof(R) == 4) {   // FP32-RHS: the dilatation alone, two points per thread
-        const dim3 grid((g.mx + 63) / 64, (g.my + 3) / 4, g.mz);
-        switch (V) {
-        case 1: k_dil_pair<1><<<grid, point_block(), 0, s>>>(g, cf, u, v, w, o.dil, own); break;
-        case 2: k_dil_pair<2><<<grid, point_block(), 0, s>>>(g, cf, u, v, w, o.dil, own); break;
-        case 3: k_dil_pair<3><<<grid, point_block(), 0, s>>>(g, cf, u, v, w, o.dil, own); break;
-        default: k_dil_pair<4><<<grid, point_block(), 0, s>>>(g, cf, u, v, w, o.dil, own); break;
-        }
-    } else {
-        switch (V) {
-        case 1: k_grad<R, 1><<<point_grid(g), point_block(), 0, s>>>(g, cf, u, v, w, o, own); break;
-        case 2: k_grad<R, 2><<<point_grid(g), point_block(), 0, s>>>(g, cf, u, v, w, o, own); break;
-        case 3: k_grad<R, 3><<<point_grid(g), point_block(), 0, s>>>(g, cf, u, v, w, o, own); break;
-        default: k_grad<R, 4><<<point_grid(g), point_block(), 0, s>>>(g, cf, u, v, w, o, own); break;
-        }
+    switch (V) {
+    case 1: k_grad<R, 1><<<point_grid(g), point_block(), 0, s>>>(g, cf, u, v, w, o, own); break;
+    case 2: k_grad<R, 2><<<point_grid(g), point_block(), 0, s>>>(g, cf, u, v, w, o, own); break;
+    case 3: k_grad<R, 3><<<point_grid(g), point_block(), 0, s>>>(g, cf, u, v, w, o, own); break;
+    default: k_grad<R, 4><<<point_grid(g), point_block(), 0, s>>>(g, cf, u, v, w, o, own); break;
+    }
+}
+void launch_dil_packed(int V, const Geom& g, const CoefT<float>& cf, const float4* qa, float* dil, int own,
+                       cudaStream_t s) {
+    switch (V) {
+    case 1: k_dil_packed<1><<<point_grid(g), point_block(), 0, s>>>(g, cf, qa, dil, own); break;
+    case 2: k_dil_packed<2><<<point_grid(g), point_block(), 0, s>>>(g, cf, qa, dil, own); break;
+    case 3: k_dil_packed<3><<<point_grid(g), point_block(), 0, s>>>(g, cf, qa, dil, own); break;
+    default: k_dil_packed<4><<<point_grid(g), point_block(), 0, s>>>(g, cf, qa, dil, own); break;
     }
 }
 template <typename R>
-int launch_reduce(const Geom& g, const Phys& ph, const StateIn& q, const R* mu, double* part, int want, double* scal,
-                  double* diag, cudaStream_t s) {
+int launch_reduce(const Geom& g, const Phys& ph, const StateIn& q, const R* mu, int mstride, double* part, int want,
+                  double* scal, double* diag, cudaStream_t s) {
     long long n = (long long)g.mx * g.my * g.mz;
     int nb = (int)((n + RED_THREADS - 1) / RED_THREADS);
     if (nb > RED_BLOCKS) nb = RED_BLOCKS;
-    k_reduce_partial<R><<<nb, RED_THREADS, 0, s>>>(g, ph, q, mu, part, want);
+    k_reduce_partial<R><<<nb, RED_THREADS, 0, s>>>(g, ph, q, mu, mstride, part, want);
     k_reduce_final<<<1, RED_THREADS, 0, s>>>(ph, part, nb, want, scal, diag);
     return 2;
 }
@@ -311,13 +255,13 @@ void launch_pack(const Geom& g, const T* src, double* dst, cudaStream_t s) {
     template void launch_ghost_state<R>(const Geom&, const Phys&, const StencilFields<R>&, const double*,          \
                                         cudaStream_t);                                                           \
     template void launch_ghost_scalar<R>(const Geom&, R*, cudaStream_t);                                          \
-    template void launch_grad<R>(int, const Geom&, const CoefT<R>&, const R*, const R*, const R*, const GradOut<R>&,  \
-                                 int, cudaStream_t);                                                             \
-    template int launch_reduce<R>(const Geom&, const Phys&, const StateIn&, const R*, double*, int, double*,      \
+    template int launch_reduce<R>(const Geom&, const Phys&, const StateIn&, const R*, int, double*, int, double*, \
                                   double*, cudaStream_t);                                                        \
     template void launch_unpack<R>(const Geom&, const double*, R*, cudaStream_t);                                 \
     template void launch_pack<R>(const Geom&, const R*, double*, cudaStream_t);
 CNS_INST(double)
 CNS_INST(float)
+template void launch_grad<double>(int, const Geom&, const CoefT<double>&, const double*, const double*, const double*,
+                                  const GradOut<double>&, int, cudaStream_t);
 
 }  // namespace cns

@@ -10,8 +10,8 @@ namespace cns {
 // ---------------------------------------------------------------------------------
 // State recovery (calcState, src/cuda_main.cu:218-242): T, p, H, mu from rho, u, v, w,
 // rhoE in FP64; stored as R (lambda = mu / (Pr Ec) is applied in the RHS). In FP32-RHS
-// mode the FP32 stencil copies of rho, u, v, w are written too and mu is evaluated in
-// FP32 from the FP64 T.
+// mode the packed records qa = (rho, u, v, w) and qb = (T, p, H, mu) are written as FP32
+// roundings and mu is evaluated in FP32 from the FP64 T rounded to FP32.
 // ---------------------------------------------------------------------------------
 // T, p, H, mu (and the FP32 copies) of one point from its FP64 state and 1/rho; the state
 // kernel and the fused epilogue of the RHS kernel share it
@@ -22,21 +22,18 @@ __device__ __forceinline__ void state_store(const Phys& ph, const DerivedOut<R>&
     const double T = ph.cvInv * en;
     const double pr = rr * ph.Rgas * T;
     const double hh = (ee + pr) * inv;
-    const R Tr = to_r<R>(T);
-    o.t[c] = Tr;
-    o.p[c] = to_r<R>(pr);
-    o.h[c] = to_r<R>(hh);
     if constexpr (sizeof(R) == 4) {
-        const float Tf = Tr;
+        const float Tf = d2f(T);
         const float suth = ph.vexp_is_one ? Tf : powf(Tf, ph.f_vexp);
-        o.m[c] = suth * ph.f_invRe;
         const float rf = d2f(rr);
-        if (o.r32) {
-            o.r32[c] = rf; o.u32[c] = d2f(uu); o.v32[c] = d2f(vv); o.w32[c] = d2f(ww);
-        }
+        o.qa[c] = make_float4(rf, d2f(uu), d2f(vv), d2f(ww));
+        o.qb[c] = make_float4(Tf, d2f(pr), d2f(hh), suth * ph.f_invRe);
         // the positivity test on the FP32 roundings keeps it off the FP64 pipe
         if (!(Tf > 0.f) || !(rf > 0.f)) scal[SC_NONFINITE] = 1.0;   // racy flag write, any writer is fine
     } else {
+        o.t[c] = T;
+        o.p[c] = pr;
+        o.h[c] = hh;
         const double suth = ph.vexp_is_one ? T : pow_visc(T, ph.vexp);
         o.m[c] = (R)(suth * ph.invRe);
         if (!(T > 0.0) || !(rr > 0.0)) scal[SC_NONFINITE] = 1.0;   // racy flag write, any writer is fine
@@ -119,9 +116,76 @@ __device__ __forceinline__ GhostCell ghost_cell_of(const Geom& g, int t) {
 // Only the six faces are filled (no stencil reads an edge or a corner). All loads of a cell
 // are issued before its stores (the eight fields may alias as far as the compiler knows).
 // ---------------------------------------------------------------------------------
+// FP32-RHS mode: the same images on the packed records qa = (rho, u, v, w), qb = (T, p, H,
+// mu), in the same FP32 arithmetic as the FP64-mode cell below with R = float
+__device__ __forceinline__ void ghost_state_cell_packed(const Geom& g, const Phys& ph, float4* __restrict__ qa,
+                                                        float4* __restrict__ qb, const double* scal, int t) {
+    const GhostCell gc = ghost_cell_of(g, t);
+    const int m = gc.m, side = gc.side;
+    long long cg, cs;
+    if (gc.face == 0) {
+        const int j = gc.j, k = gc.k;
+        cg = g.at(side == 0 ? -m : g.mx - 1 + m, j, k);
+        if (g.xbc != XBC_PER) {
+            const long long cp = g.at(side == 0 ? m - 1 : g.mx - m, j, k);
+            float ug, vg, wg, pg, Tg;
+            if (g.xbc == XBC_WALL) {
+                const double Tw = side == 0 ? ph.twall_bot : ph.twall_top;
+                const float4 a = qa[cp], b = qb[cp];
+                ug = -a.y; vg = -a.z; wg = -a.w;
+                pg = b.y;
+                Tg = (float)(2.0 * Tw) - b.x;
+            } else if (side == 0) {   // boundary layer, wall
+                const float4 a = qa[cp], b = qb[cp];
+                ug = -a.y; vg = -a.z; wg = -a.w;
+                pg = b.y;
+                Tg = b.x;
+                double pv;
+                if (ph.perturbed && wall_perturbation(ph, g.dy, j, k, scal[SC_TIME], &pv)) ug = d2f(pv);
+            } else {                  // boundary layer, free stream: extrapolate through the last node
+                const long long cl = g.at(g.mx - 1, j, k);
+                const long long cm = g.at(g.mx - 1 - m, j, k);
+                const float4 al = qa[cl], am = qa[cm], bl = qb[cl], bm = qb[cm];
+                ug = 2.0f * al.y - am.y;
+                vg = 2.0f * al.z - am.z;
+                wg = 2.0f * al.w - am.w;
+                pg = 2.0f * bl.y - bm.y;
+                Tg = 2.0f * bl.x - bm.x;
+            }
+            const float suth = ph.vexp_is_one ? Tg : powf(Tg, (float)ph.vexp);
+            const float hg = Tg * (float)ph.hcoef + 0.5f * (ug * ug + vg * vg + wg * wg);
+            qa[cg] = make_float4(pg / ((float)ph.Rgas * Tg), ug, vg, wg);
+            qb[cg] = make_float4(Tg, pg, hg, suth * (float)ph.invRe);
+            return;
+        }
+        cs = g.at(side == 0 ? g.mx - m : m - 1, j, k);
+    } else if (gc.face == 1) {
+        cg = g.at(gc.i, side == 0 ? -m : g.my - 1 + m, gc.k);
+        cs = g.at(gc.i, side == 0 ? g.my - m : m - 1, gc.k);
+    } else {
+        cg = g.at(gc.i, gc.j, side == 0 ? -m : g.mz - 1 + m);
+        if (g.zbl) {
+            const long long c0 = g.at(gc.i, gc.j, side == 0 ? 0 : g.mz - 1);
+            const long long cm = g.at(gc.i, gc.j, side == 0 ? m : g.mz - 1 - m);
+            const float4 a0 = qa[c0], am = qa[cm], b0 = qb[c0], bm = qb[cm];
+            qa[cg] = make_float4(2.0f * a0.x - am.x, 2.0f * a0.y - am.y, 2.0f * a0.z - am.z, 2.0f * a0.w - am.w);
+            qb[cg] = make_float4(2.0f * b0.x - bm.x, 2.0f * b0.y - bm.y, 2.0f * b0.z - bm.z, 2.0f * b0.w - bm.w);
+            return;
+        }
+        cs = g.at(gc.i, gc.j, side == 0 ? g.mz - m : m - 1);
+    }
+    const float4 a = qa[cs], b = qb[cs];
+    qa[cg] = a;
+    qb[cg] = b;
+}
+
 template <typename R>
 __device__ __forceinline__ void ghost_state_cell(const Geom& g, const Phys& ph, const StencilFields<R>& f,
                                                  const double* scal, int t) {
+    if constexpr (sizeof(R) == 4) {
+        ghost_state_cell_packed(g, ph, f.qa, f.qb, scal, t);
+        return;
+    }
     R* F[8] = {f.r, f.u, f.v, f.w, f.t, f.p, f.h, f.m};
     const GhostCell gc = ghost_cell_of(g, t);
     const int m = gc.m, side = gc.side;
@@ -295,6 +359,29 @@ __device__ __forceinline__ void grad_point(const Geom& g, const CoefT<R>& cf, co
     const R th = out[0] + out[4] + out[8];
     o.dil[c] = th;
     if (own) dil_ghost_owner<R>(g, o.dil, c, i, j, k, th);
+}
+
+// FP32-RHS dilatation from the packed records qa = (rho, u, v, w): the diagonal gradients
+// du/dx, dv/dy, dw/dz at the viscous order (grad_point's DIL_ONLY arithmetic) and theta.
+template <int V>
+__device__ __forceinline__ void dil_point_packed(const Geom& g, const CoefT<float>& cf,
+                                                 const float4* __restrict__ qa, float* __restrict__ dil, int i, int j,
+                                                 int k, bool own = false) {
+    const int c = (int)g.at(i, j, k);
+    const int P = (int)g.P, PS = (int)g.PS;
+    float sx = cf.c1V[0][1] * (__ldg(qa + c + 1).y - __ldg(qa + c - 1).y);
+    float sy = cf.c1V[1][1] * (__ldg(qa + c + P).z - __ldg(qa + c - P).z);
+    float sz = cf.c1V[2][1] * (__ldg(qa + c + PS).w - __ldg(qa + c - PS).w);
+#pragma unroll
+    for (int kk = 2; kk <= V; kk++) {
+        sx = fma(cf.c1V[0][kk], __ldg(qa + c + kk).y - __ldg(qa + c - kk).y, sx);
+        sy = fma(cf.c1V[1][kk], __ldg(qa + c + kk * P).z - __ldg(qa + c - kk * P).z, sy);
+        sz = fma(cf.c1V[2][kk], __ldg(qa + c + kk * PS).w - __ldg(qa + c - kk * PS).w, sz);
+    }
+    if (g.nonuniform_x) sx *= cf.xp[i];
+    const float th = sx + sy + sz;
+    dil[c] = th;
+    if (own) dil_ghost_owner<float>(g, dil, c, i, j, k, th);
 }
 
 // Dilatation ghost cell t (BCxNumber2 / BCyNumber1 / BCzNumber1): x periodic | wall:

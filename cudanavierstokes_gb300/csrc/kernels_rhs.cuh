@@ -219,49 +219,12 @@ __device__ __forceinline__ void rhs_direction(const Geom& g, const CoefT<R>& cf,
     acc[1 + DIR] -= dp;
 }
 
-// RHS + stage update of one interior point (i, ., k) at element c, with the neighbours
-// along x, y, z from the accessors nx, ny, nz and the centre values given
-template <typename R, int S, int V, class NX, class NY, class NZ>
-__device__ __forceinline__ void rhs_point_nb(const Geom& g, const CoefT<R>& cf, const RhsIn<R>& in,
-                                             const Update<R>& up, double* __restrict__ scal, int quirk, int i,
-                                             int k, int c, const NX& nx, const NY& ny, const NZ& nz, R th0,
-                                             R m0, R u0, R v0, R w0, R r0, R h0) {
-    R Gr[9];
-    if constexpr (sizeof(R) == 8) {   // FP64: the gradient kernel's fields; FP32: formed in the passes
-#pragma unroll
-        for (int q = 0; q < 9; q++) Gr[q] = ld(in.g[q], c);
-    }
-    const R m3 = m0 * (R)(1.0 / 3.0);
-    R acc[5] = {0, 0, 0, 0, 0};
-    R W[3] = {0, 0, 0};
-    R diss = 0, cond = 0;
-    R dmu[3];
-    rhs_direction<R, S, V, 0>(g, cf, nx, i, Gr, th0, m0, m3, u0, v0, w0, r0, h0, quirk, acc, W, diss, cond, dmu[0]);
-    rhs_direction<R, S, V, 1>(g, cf, ny, i, Gr, th0, m0, m3, u0, v0, w0, r0, h0, quirk, acc, W, diss, cond, dmu[1]);
-    rhs_direction<R, S, V, 2>(g, cf, nz, i, Gr, th0, m0, m3, u0, v0, w0, r0, h0, quirk, acc, W, diss, cond, dmu[2]);
-    if constexpr (sizeof(R) == 4) {
-        // stress rows, dissipation and grad(mu) . s of every direction, now that all nine
-        // gradients are known
-#pragma unroll
-        for (int d = 0; d < 3; d++) {
-            R tau[3];
-#pragma unroll
-            for (int q = 0; q < 3; q++)
-                tau[q] = (q == d) ? (R)2 * Gr[3 * d + q] - (R)(2. / 3.) * th0 : Gr[3 * d + q] + Gr[3 * q + d];
-            const R dw = (d == 1 && quirk) ? Gr[7] : Gr[3 * d + 2];
-            diss = fma(tau[0], Gr[3 * d + 0], diss);
-            diss = fma(tau[1], Gr[3 * d + 1], diss);
-            diss = fma(tau[2], dw, diss);
-            W[0] = fma(tau[0], dmu[d], W[0]);
-            W[1] = fma(tau[1], dmu[d], W[1]);
-            W[2] = fma(tau[2], dmu[d], W[2]);
-        }
-    }
-    acc[1] += W[0];
-    acc[2] += W[1];
-    acc[3] += W[2];
-    acc[4] += fma(m0, diss, cf.lam_mu * cond) + fma(u0, W[0], fma(v0, W[1], w0 * W[2]));
-
+// Body force, sponge, stage update and the new state's recovery of the point at element
+// c, given its RHS accumulators acc (convective, pressure and viscous terms) and centre
+// values u0, v0, w0, r0 in the arithmetic type R
+template <typename R>
+__device__ __forceinline__ void stage_tail(const Geom& g, const Update<R>& up, double* __restrict__ scal, int i, int k,
+                                           int c, R (&acc)[5], R u0, R v0, R w0, R r0) {
     // ---- body force and sponge (RHS terms, arithmetic type R) ----
     const R dpdz = to_r<R>(scal[SC_DPDZ]);
     acc[3] += dpdz;
@@ -352,15 +315,214 @@ __device__ __forceinline__ void rhs_point_nb(const Geom& g, const CoefT<R>& cf, 
     if (up.fuse) state_store<R>(up.ph, up.dnext, scal, c, qn[0], inv, un, vn, wn, qn[4]);
 }
 
+// RHS + stage update of one interior point (i, ., k) at element c, with the neighbours
+// along x, y, z from the accessors nx, ny, nz and the centre values given
+template <typename R, int S, int V, class NX, class NY, class NZ>
+__device__ __forceinline__ void rhs_point_nb(const Geom& g, const CoefT<R>& cf, const RhsIn<R>& in,
+                                             const Update<R>& up, double* __restrict__ scal, int quirk, int i,
+                                             int k, int c, const NX& nx, const NY& ny, const NZ& nz, R th0,
+                                             R m0, R u0, R v0, R w0, R r0, R h0) {
+    R Gr[9];
+    if constexpr (sizeof(R) == 8) {   // FP64: the gradient kernel's fields; FP32: formed in the passes
+#pragma unroll
+        for (int q = 0; q < 9; q++) Gr[q] = ld(in.g[q], c);
+    }
+    const R m3 = m0 * (R)(1.0 / 3.0);
+    R acc[5] = {0, 0, 0, 0, 0};
+    R W[3] = {0, 0, 0};
+    R diss = 0, cond = 0;
+    R dmu[3];
+    rhs_direction<R, S, V, 0>(g, cf, nx, i, Gr, th0, m0, m3, u0, v0, w0, r0, h0, quirk, acc, W, diss, cond, dmu[0]);
+    rhs_direction<R, S, V, 1>(g, cf, ny, i, Gr, th0, m0, m3, u0, v0, w0, r0, h0, quirk, acc, W, diss, cond, dmu[1]);
+    rhs_direction<R, S, V, 2>(g, cf, nz, i, Gr, th0, m0, m3, u0, v0, w0, r0, h0, quirk, acc, W, diss, cond, dmu[2]);
+    if constexpr (sizeof(R) == 4) {
+        // stress rows, dissipation and grad(mu) . s of every direction, now that all nine
+        // gradients are known
+#pragma unroll
+        for (int d = 0; d < 3; d++) {
+            R tau[3];
+#pragma unroll
+            for (int q = 0; q < 3; q++)
+                tau[q] = (q == d) ? (R)2 * Gr[3 * d + q] - (R)(2. / 3.) * th0 : Gr[3 * d + q] + Gr[3 * q + d];
+            const R dw = (d == 1 && quirk) ? Gr[7] : Gr[3 * d + 2];
+            diss = fma(tau[0], Gr[3 * d + 0], diss);
+            diss = fma(tau[1], Gr[3 * d + 1], diss);
+            diss = fma(tau[2], dw, diss);
+            W[0] = fma(tau[0], dmu[d], W[0]);
+            W[1] = fma(tau[1], dmu[d], W[1]);
+            W[2] = fma(tau[2], dmu[d], W[2]);
+        }
+    }
+    acc[1] += W[0];
+    acc[2] += W[1];
+    acc[3] += W[2];
+    acc[4] += fma(m0, diss, cf.lam_mu * cond) + fma(u0, W[0], fma(v0, W[1], w0 * W[2]));
+
+    stage_tail<R>(g, up, scal, i, k, c, acc, u0, v0, w0, r0);
+}
+
+// ---------------------------------------------------------------------------------
+// FP32-RHS point body on the packed stencil records qa = (rho, u, v, w), qb = (T, p, H, mu)
+// and theta. One pass per direction walks the offsets l = 1..S once: at each l it loads
+// the two records on either side (four 16-byte loads) and theta (for l <= V) and feeds
+// every sum that needs them -- the first derivatives of u, v, w, mu, T, theta at the
+// viscous order and of p at the advective order, the second derivatives of u, v, w, T, and
+// the telescoped split-form fluxes -- so no stencil is held in registers. Each sum is
+// accumulated in the order of the FP64-mode body (centre term, then l ascending) with the
+// same expressions; the non-uniform x second derivative adds the pair (l, -l) per l.
+// ---------------------------------------------------------------------------------
+template <int S, int V, int DIR>
+__device__ __forceinline__ void rhs_dir_packed(const Geom& g, const CoefT<float>& cf, const RhsIn<float>& in, int c,
+                                               int st, int i, float (&Gr)[9], float m0, float m3, float u0, float v0,
+                                               float w0, float r0, float h0, float T0, float (&acc)[5],
+                                               float (&W)[3], float& cond, float& dmu_dir) {
+    static_assert(V <= S, "the viscous half-width never exceeds the advective one");
+    const bool nux = (DIR == 0) && g.nonuniform_x;
+    const float xpi = nux ? cf.xp[i] : 1.0f;
+    const float* c1V = cf.c1V[DIR];
+    const float* c1S = cf.c1S[DIR];
+    const float* c2V = cf.c2V[DIR];
+    const float* fq = cf.fq[DIR];
+    const float* fcb = cf.fc[DIR];
+    const float un = DIR == 0 ? u0 : (DIR == 1 ? v0 : w0);
+
+    float gu = 0.f, gv = 0.f, gw = 0.f, dmu = 0.f, dT = 0.f, dth = 0.f, dp = 0.f;
+    float d2uu, d2vv, d2ww, d2tt;
+    if (nux) {
+        const float cw = __ldg(cf.cvsx + V * g.mx + i);
+        d2uu = cw * u0; d2vv = cw * v0; d2ww = cw * w0; d2tt = cw * T0;
+    } else {
+        d2uu = c2V[0] * u0; d2vv = c2V[0] * v0; d2ww = c2V[0] * w0; d2tt = c2V[0] * T0;
+    }
+    float sq = 0.f, fu = nux ? 0.f : acc[1], fv = nux ? 0.f : acc[2], fw = nux ? 0.f : acc[3],
+          fe = nux ? 0.f : acc[4];
+#pragma unroll
+    for (int l = 1; l <= S; l++) {
+        const float4 Ap = __ldg(in.qa + c + l * st), Am = __ldg(in.qa + c - l * st);
+        const float4 Bp = __ldg(in.qb + c + l * st), Bm = __ldg(in.qb + c - l * st);
+        if (l <= V) {
+            const float thp = __ldg(in.dil + c + l * st), thm = __ldg(in.dil + c - l * st);
+            if (l == 1) {
+                gu = c1V[1] * (Ap.y - Am.y); gv = c1V[1] * (Ap.z - Am.z); gw = c1V[1] * (Ap.w - Am.w);
+                dmu = c1V[1] * (Bp.w - Bm.w); dT = c1V[1] * (Bp.x - Bm.x); dth = c1V[1] * (thp - thm);
+            } else {
+                gu = fma(c1V[l], Ap.y - Am.y, gu); gv = fma(c1V[l], Ap.z - Am.z, gv);
+                gw = fma(c1V[l], Ap.w - Am.w, gw);
+                dmu = fma(c1V[l], Bp.w - Bm.w, dmu); dT = fma(c1V[l], Bp.x - Bm.x, dT);
+                dth = fma(c1V[l], thp - thm, dth);
+            }
+            if (nux) {
+                const float cp = __ldg(cf.cvsx + (V + l) * g.mx + i), cm = __ldg(cf.cvsx + (V - l) * g.mx + i);
+                d2uu = fma(cp, Ap.y, fma(cm, Am.y, d2uu));
+                d2vv = fma(cp, Ap.z, fma(cm, Am.z, d2vv));
+                d2ww = fma(cp, Ap.w, fma(cm, Am.w, d2ww));
+                d2tt = fma(cp, Bp.x, fma(cm, Bm.x, d2tt));
+            } else {
+                d2uu = fma(c2V[l], Ap.y + Am.y, d2uu);
+                d2vv = fma(c2V[l], Ap.z + Am.z, d2vv);
+                d2ww = fma(c2V[l], Ap.w + Am.w, d2ww);
+                d2tt = fma(c2V[l], Bp.x + Bm.x, d2tt);
+            }
+        }
+        dp = l == 1 ? c1S[1] * (Bp.y - Bm.y) : fma(c1S[l], Bp.y - Bm.y, dp);
+        // telescoped split-form fluxes (rhs_direction: a_l Q+- shared by the cubic fluxes)
+        const float gm = DIR == 0 ? Am.y : (DIR == 1 ? Am.z : Am.w);
+        const float gp = DIR == 0 ? Ap.y : (DIR == 1 ? Ap.z : Ap.w);
+        const float Qm = (Am.x + r0) * (gm + un);
+        const float Qp = (r0 + Ap.x) * (un + gp);
+        sq = fma(fq[l], Qm - Qp, sq);
+        const float am = fcb[l] * Qm, ap = fcb[l] * Qp;
+        fu = fma(am, Am.y, fma(-ap, Ap.y, fu));
+        fv = fma(am, Am.z, fma(-ap, Ap.z, fv));
+        fw = fma(am, Am.w, fma(-ap, Ap.w, fw));
+        fe = fma(am, Bm.z, fma(-ap, Bp.z, fe));
+    }
+    if (nux) { gu *= xpi; gv *= xpi; gw *= xpi; }
+    Gr[3 * DIR + 0] = gu; Gr[3 * DIR + 1] = gv; Gr[3 * DIR + 2] = gw;
+    dmu *= xpi;
+    dmu_dir = dmu;
+    W[0] = fma(d2uu, m0, W[0]);
+    W[1] = fma(d2vv, m0, W[1]);
+    W[2] = fma(d2ww, m0, W[2]);
+    // heat conduction (lambda / mu)(mu d2T + dmu dT), the ratio applied once per point
+    dT *= xpi;
+    cond = fma(d2tt, m0, cond);
+    cond = fma(dT, dmu, cond);
+    dth *= xpi;
+    dp *= xpi;
+    W[DIR] = fma(m3, dth, W[DIR]);
+    const float half = 0.5f * sq;
+    fu = fma(u0, half, fu);
+    fv = fma(v0, half, fv);
+    fw = fma(w0, half, fw);
+    fe = fma(h0, half, fe);
+    const float fr = nux ? sq : acc[0] + sq;
+    if (nux) {
+        acc[0] = fma(xpi, fr, acc[0]);
+        acc[1] = fma(xpi, fu, acc[1]);
+        acc[2] = fma(xpi, fv, acc[2]);
+        acc[3] = fma(xpi, fw, acc[3]);
+        acc[4] = fma(xpi, fe, acc[4]);
+    } else {
+        acc[0] = fr; acc[1] = fu; acc[2] = fv; acc[3] = fw; acc[4] = fe;
+    }
+    acc[1 + DIR] -= dp;
+}
+
+template <int S, int V>
+__device__ __forceinline__ void rhs_point_packed(const Geom& g, const CoefT<float>& cf, const RhsIn<float>& in,
+                                                 const Update<float>& up, double* __restrict__ scal, int quirk, int i,
+                                                 int j, int k) {
+    const int c = (int)g.at(i, j, k);
+    const float4 A0 = __ldg(in.qa + c), B0 = __ldg(in.qb + c);
+    const float th0 = __ldg(in.dil + c);
+    const float r0 = A0.x, u0 = A0.y, v0 = A0.z, w0 = A0.w;
+    const float T0 = B0.x, h0 = B0.z, m0 = B0.w;
+    const float m3 = m0 * (float)(1.0 / 3.0);
+    float Gr[9];
+    float acc[5] = {0, 0, 0, 0, 0};
+    float W[3] = {0, 0, 0};
+    float diss = 0, cond = 0;
+    float dmu[3];
+    rhs_dir_packed<S, V, 0>(g, cf, in, c, 1, i, Gr, m0, m3, u0, v0, w0, r0, h0, T0, acc, W, cond, dmu[0]);
+    rhs_dir_packed<S, V, 1>(g, cf, in, c, (int)g.P, i, Gr, m0, m3, u0, v0, w0, r0, h0, T0, acc, W, cond, dmu[1]);
+    rhs_dir_packed<S, V, 2>(g, cf, in, c, (int)g.PS, i, Gr, m0, m3, u0, v0, w0, r0, h0, T0, acc, W, cond, dmu[2]);
+    // stress rows, dissipation and grad(mu) . s of every direction, now that all nine
+    // gradients are known (y: tau_yz dv/dz with the quirk, src/cuda_rhs.cu:175)
+#pragma unroll
+    for (int d = 0; d < 3; d++) {
+        float tau[3];
+#pragma unroll
+        for (int q = 0; q < 3; q++)
+            tau[q] = (q == d) ? 2.0f * Gr[3 * d + q] - (float)(2. / 3.) * th0 : Gr[3 * d + q] + Gr[3 * q + d];
+        const float dw = (d == 1 && quirk) ? Gr[7] : Gr[3 * d + 2];
+        diss = fma(tau[0], Gr[3 * d + 0], diss);
+        diss = fma(tau[1], Gr[3 * d + 1], diss);
+        diss = fma(tau[2], dw, diss);
+        W[0] = fma(tau[0], dmu[d], W[0]);
+        W[1] = fma(tau[1], dmu[d], W[1]);
+        W[2] = fma(tau[2], dmu[d], W[2]);
+    }
+    acc[1] += W[0];
+    acc[2] += W[1];
+    acc[3] += W[2];
+    acc[4] += fma(m0, diss, cf.lam_mu * cond) + fma(u0, W[0], fma(v0, W[1], w0 * W[2]));
+    stage_tail<float>(g, up, scal, i, k, c, acc, u0, v0, w0, r0);
+}
+
 // RHS + stage update of one interior point (i, j, k), every neighbour from global memory
 template <typename R, int S, int V>
 __device__ __forceinline__ void rhs_point(const Geom& g, const CoefT<R>& cf, const RhsIn<R>& in, const Update<R>& up,
                                           double* __restrict__ scal, int quirk, int i, int j, int k) {
-    const int c = (int)g.at(i, j, k);
-    const R th0 = ld(in.dil, c), m0 = ld(in.m, c);
-    const R u0 = ld(in.u, c), v0 = ld(in.v, c), w0 = ld(in.w, c), r0 = ld(in.r, c), h0 = ld(in.h, c);
-    const NbGlobal<R> nx{&in, c, 1}, ny{&in, c, (int)g.P}, nz{&in, c, (int)g.PS};
-    rhs_point_nb<R, S, V>(g, cf, in, up, scal, quirk, i, k, c, nx, ny, nz, th0, m0, u0, v0, w0, r0, h0);
+    if constexpr (sizeof(R) == 4) {
+        rhs_point_packed<S, V>(g, cf, in, up, scal, quirk, i, j, k);
+    } else {
+        const int c = (int)g.at(i, j, k);
+        const R th0 = ld(in.dil, c), m0 = ld(in.m, c);
+        const R u0 = ld(in.u, c), v0 = ld(in.v, c), w0 = ld(in.w, c), r0 = ld(in.r, c), h0 = ld(in.h, c);
+        const NbGlobal<R> nx{&in, c, 1}, ny{&in, c, (int)g.P}, nz{&in, c, (int)g.PS};
+        rhs_point_nb<R, S, V>(g, cf, in, up, scal, quirk, i, k, c, nx, ny, nz, th0, m0, u0, v0, w0, r0, h0);
+    }
 }
 
 // FP32: 7 blocks of 128 per SM (72 registers) measured fastest (6: 80 registers, +13 %

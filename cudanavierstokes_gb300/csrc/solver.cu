@@ -105,16 +105,17 @@ int check_params(const cns_params* p) {
 
 template <typename R>
 RhsIn<R> rhs_in(cns_solver* h, int c) {
-    RhsIn<R> in;
-    if (h->fp32) {
-        in.r = (const R*)h->s32[c][0]; in.u = (const R*)h->s32[c][1]; in.v = (const R*)h->s32[c][2];
-        in.w = (const R*)h->s32[c][3];
+    RhsIn<R> in{};
+    if (h->fp32) {   // packed records (rho, u, v, w) and (T, p, H, mu)
+        in.qa = (const float4*)h->der[c][0];
+        in.qb = (const float4*)h->der[c][1];
     } else {
         in.r = (const R*)h->q[c][0]; in.u = (const R*)h->q[c][1]; in.v = (const R*)h->q[c][2]; in.w = (const R*)h->q[c][3];
+        in.h = (const R*)h->der[c][0]; in.t = (const R*)h->der[c][1]; in.p = (const R*)h->der[c][2];
+        in.m = (const R*)h->der[c][3];
+        for (int q = 0; q < 9; q++) in.g[q] = (const R*)h->grad[q];
     }
-    in.h = (const R*)h->der[c][0]; in.t = (const R*)h->der[c][1]; in.p = (const R*)h->der[c][2];
-    in.m = (const R*)h->der[c][3]; in.dil = (const R*)h->dil;
-    for (int q = 0; q < 9; q++) in.g[q] = (const R*)h->grad[q];
+    in.dil = (const R*)h->dil;
     return in;
 }
 
@@ -125,11 +126,12 @@ StateIn state_in(cns_solver* h, int b) {
 // derived-field outputs of state buffer b
 template <typename R>
 DerivedOut<R> derived_out(cns_solver* h, int b) {
-    DerivedOut<R> o;
-    o.h = (R*)h->der[b][0]; o.t = (R*)h->der[b][1]; o.p = (R*)h->der[b][2]; o.m = (R*)h->der[b][3];
-    o.r32 = o.u32 = o.v32 = o.w32 = nullptr;
+    DerivedOut<R> o{};
     if (h->fp32) {
-        o.r32 = (R*)h->s32[b][0]; o.u32 = (R*)h->s32[b][1]; o.v32 = (R*)h->s32[b][2]; o.w32 = (R*)h->s32[b][3];
+        o.qa = (float4*)h->der[b][0];
+        o.qb = (float4*)h->der[b][1];
+    } else {
+        o.h = (R*)h->der[b][0]; o.t = (R*)h->der[b][1]; o.p = (R*)h->der[b][2]; o.m = (R*)h->der[b][3];
     }
     return o;
 }
@@ -151,13 +153,13 @@ template <typename R>
 int ghost_phase(cns_solver* h) {
     const int c = h->cur;
     const DerivedOut<R> o = derived_out<R>(h, c);
-    StencilFields<R> f;
+    StencilFields<R> f{};
     if (h->fp32) {
-        f.r = o.r32; f.u = o.u32; f.v = o.v32; f.w = o.w32;
+        f.qa = o.qa; f.qb = o.qb;
     } else {
         f.r = (R*)h->q[c][0]; f.u = (R*)h->q[c][1]; f.v = (R*)h->q[c][2]; f.w = (R*)h->q[c][3];
+        f.t = o.t; f.p = o.p; f.h = o.h; f.m = o.m;
     }
-    f.t = o.t; f.p = o.p; f.h = o.h; f.m = o.m;
     launch_ghost_state<R>(h->geom, h->phys, f, h->scal, h->stream);
     h->launches += 1;
     CKL();
@@ -166,19 +168,21 @@ int ghost_phase(cns_solver* h) {
 
 template <typename R>
 int grad_phase(cns_solver* h) {
-    GradOut<R> o;
-    for (int q = 0; q < 9; q++) o.g[q] = (R*)h->grad[q];
-    o.dil = (R*)h->dil;
-    const R *u, *v, *w;
-    if (h->fp32) { u = (const R*)h->s32[h->cur][1]; v = (const R*)h->s32[h->cur][2]; w = (const R*)h->s32[h->cur][3]; }
-    else { u = (const R*)h->q[h->cur][1]; v = (const R*)h->q[h->cur][2]; w = (const R*)h->q[h->cur][3]; }
-    const CoefT<R>* cfp;
-    if constexpr (std::is_same<R, float>::value) cfp = &h->cf32; else cfp = &h->cf64;
-    const CoefT<R>& cf = *cfp;
     // every dilatation ghost is a copy of one interior value unless the boundary layer
     // extrapolates: then the gradient kernel writes them itself
     const bool own = h->geom.xbc != XBC_BL && !h->geom.zbl;
-    launch_grad<R>(h->p.stencil_visc, h->geom, cf, u, v, w, o, own ? 1 : 0, h->stream);
+    if constexpr (std::is_same<R, float>::value) {   // FP32-RHS: theta alone, from the packed records
+        launch_dil_packed(h->p.stencil_visc, h->geom, h->cf32, (const float4*)h->der[h->cur][0], (float*)h->dil,
+                          own ? 1 : 0, h->stream);
+    } else {
+        GradOut<R> o;
+        for (int q = 0; q < 9; q++) o.g[q] = (R*)h->grad[q];
+        o.dil = (R*)h->dil;
+        const R* u = (const R*)h->q[h->cur][1];
+        const R* v = (const R*)h->q[h->cur][2];
+        const R* w = (const R*)h->q[h->cur][3];
+        launch_grad<R>(h->p.stencil_visc, h->geom, h->cf64, u, v, w, o, own ? 1 : 0, h->stream);
+    }
     h->launches += 1;
     if (!own) {
         launch_ghost_scalar<R>(h->geom, (R*)h->dil, h->stream);
@@ -269,10 +273,11 @@ int solver_ensure_state(cns_solver* h) { return ensure_state(h); }
 }  // namespace cns
 
 int cns::solver_reduce(cns_solver* h, int want, double* diag) {
-    if (h->fp32) launch_reduce<float>(h->geom, h->phys, state_in(h, h->cur), (const float*)h->der[h->mu_buf][3], h->part, want,
-                                      h->scal, diag, h->stream);
-    else launch_reduce<double>(h->geom, h->phys, state_in(h, h->cur), (const double*)h->der[h->mu_buf][3], h->part, want,
-                               h->scal, diag, h->stream);
+    if (h->fp32)   // mu is the fourth value of the packed record (T, p, H, mu)
+        launch_reduce<float>(h->geom, h->phys, state_in(h, h->cur), (const float*)h->der[h->mu_buf][1] + 3, 4, h->part,
+                             want, h->scal, diag, h->stream);
+    else launch_reduce<double>(h->geom, h->phys, state_in(h, h->cur), (const double*)h->der[h->mu_buf][3], 1, h->part,
+                               want, h->scal, diag, h->stream);
     h->launches += 2;
     CKL();
     return CNS_OK;
@@ -489,9 +494,10 @@ int cns_create(const cns_params* pin, int device, cns_solver** out) {
     for (int b = 0; b < 2 && !rc; b++)
         for (int f = 0; f < 5 && !rc; f++) rc = h->alloc_field((void**)&h->q[b][f], 8);
     for (int b = 0; b < 2; b++) {
-        for (int f = 0; f < 4 && !rc; f++) rc = h->alloc_field(&h->der[b][f], rs);
-        if (!rc && h->fp32)
-            for (int f = 0; f < 4 && !rc; f++) rc = h->alloc_field(&h->s32[b][f], 4);
+        if (h->fp32)   // packed FP32 records (rho, u, v, w) and (T, p, H, mu)
+            for (int f = 0; f < 2 && !rc; f++) rc = h->alloc_field(&h->der[b][f], sizeof(float4));
+        else
+            for (int f = 0; f < 4 && !rc; f++) rc = h->alloc_field(&h->der[b][f], rs);
     }
     if (!rc) rc = h->alloc_field(&h->dil, rs);
     if (!h->fp32)   // FP32-RHS: the RHS kernel forms the velocity gradients itself

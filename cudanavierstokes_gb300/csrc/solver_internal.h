@@ -35,12 +35,12 @@ struct cns_solver {
 
     double* q[2][5] = {};        // state ping-pong (rho, u, v, w, rhoE)
     int cur = 0;
-    // derived fields h, t, p, mu (R) and the FP32 stencil copies of rho, u, v, w of the
-    // state buffer q[b], in der[b] / s32[b]: the RHS kernel reads those of q[cur] and writes
-    // those of the new state q[1 - cur] (fused state recovery)
+    // stencil inputs derived from the state buffer q[b], in der[b]: FP64 mode h, t, p, mu
+    // (the state itself gives rho, u, v, w); FP32-RHS mode der[b][0] = the packed records
+    // (rho, u, v, w) and der[b][1] = (T, p, H, mu), float4 each. The RHS kernel reads those of
+    // q[cur] and writes those of the new state q[1 - cur] (fused state recovery)
     void* der[2][4] = {};
-    void* s32[2][4] = {};
-    bool der_ok[2] = {false, false};   // der[b] / s32[b] hold the recovery of q[b]
+    bool der_ok[2] = {false, false};   // der[b] holds the recovery of q[b]
     int mu_buf = 0;                    // buffer of the latest state recovery in program order of
                                        // the reference (its mu sets the CFL time step)
     void* dil = nullptr;         // (R)
@@ -119,7 +119,6 @@ inline void solver_set_parity(cns_solver* h, int want) {
     }
     for (int f = 0; f < 4; f++) {
         void* a = h->der[0][f]; h->der[0][f] = h->der[1][f]; h->der[1][f] = a;
-        void* b = h->s32[0][f]; h->s32[0][f] = h->s32[1][f]; h->s32[1][f] = b;
     }
     const bool ok0 = h->der_ok[0];
     h->der_ok[0] = h->der_ok[1];
