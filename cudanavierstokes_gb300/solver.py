@@ -150,7 +150,7 @@ class Solver:
         """Per-phase device time (ms) averaged over nstages low-storage stages."""
         ms = np.zeros(3)
         native.check(native.lib().cns_time_phases(self._h, int(nstages), _ptr(ms)))
-        return dict(state_ms=float(ms[0]), grad_ms=float(ms[1]), rhs_ms=float(ms[2]))
+        return dict(ghost_ms=float(ms[0]), grad_ms=float(ms[1]), rhs_ms=float(ms[2]))
 
     @property
     def kernel_launches(self) -> int:
