@@ -32,9 +32,11 @@ using namespace cns;
 
 namespace cns {
 void launch_batch_stage_fp64(int S, int V, dim3 grid, const BatchInst<double>* tab, const BatchCtl* ctl, int cur,
-                             int stage, int quirk, unsigned* bar, int* err, cudaStream_t s);
+                             int stage, int quirk, unsigned* bar, int* err, unsigned long long* cnt,
+                             const RhsTable<double>& rt, cudaStream_t s);
 void launch_batch_stage_fp32(int S, int V, dim3 grid, const BatchInst<float>* tab, const BatchCtl* ctl, int cur,
-                             int stage, int quirk, unsigned* bar, int* err, cudaStream_t s);
+                             int stage, int quirk, unsigned* bar, int* err, unsigned long long* cnt,
+                             const RhsTable<float>& rt, cudaStream_t s);
 void launch_batch_time_fp64(const BatchInst<double>* tab, const BatchCtl* ctl, cudaStream_t s);
 void launch_batch_time_fp32(const BatchInst<float>* tab, const BatchCtl* ctl, cudaStream_t s);
 int batch_stage_occupancy(int fp32, int S, int V, int* blocks_per_sm);
@@ -85,6 +87,8 @@ struct cns_batch {
     void* d_tab = nullptr;
     BatchCtl* d_ctl = nullptr;
     unsigned* d_bar = nullptr;
+    unsigned long long* d_cnt = nullptr;   // the persistent kernel's four phase unit counters
+    std::vector<BatchInst<float>> h_tab32;   // host copy of the FP32 member table (RHS-phase argument)
     int* d_err = nullptr;
     int threads = 128, blocks_per_sm = 1, nsm = 152;
     bool tuned = false;
@@ -106,6 +110,7 @@ struct cns_batch {
         if (d_tab) cudaFree(d_tab);
         if (d_ctl) cudaFree(d_ctl);
         if (d_bar) cudaFree(d_bar);
+        if (d_cnt) cudaFree(d_cnt);
         if (d_err) cudaFree(d_err);
         for (auto s : lanes) cudaStreamDestroy(s);
         for (auto e : lane_done) cudaEventDestroy(e);
@@ -184,12 +189,50 @@ int upload_table(cns_batch* b) {
     BCK(cudaMemcpyAsync(b->d_tab, tab.data(), sizeof(BatchInst<R>) * n, cudaMemcpyHostToDevice, b->stream));
     BCK(cudaMemcpyAsync(b->d_ctl, &ctl, sizeof ctl, cudaMemcpyHostToDevice, b->stream));
     BCK(cudaStreamSynchronize(b->stream));
+    if constexpr (sizeof(R) == 4) {
+        // the RHS phase's member table is a launch argument, baked into the captured steps
+        b->h_tab32.assign(tab.begin(), tab.begin() + n);
+        b->drop_graphs();
+    }
     b->dirty = false;
     return CNS_OK;
 }
 
 int upload(cns_batch* b) {
     return b->precision == CNS_PREC_FP32_RHS ? upload_table<float>(b) : upload_table<double>(b);
+}
+
+// The RHS phase's member table for stage s from parity cur: FP32 batches of up to
+// RHS_TABLE_MAX members (n = 0 otherwise: the kernel stages the parameters in shared memory)
+RhsTable<float> rhs_table(const cns_batch* b, int s, int cur) {
+    RhsTable<float> t;
+    std::memset(&t, 0, sizeof t);
+    const int n = (int)b->h_tab32.size();
+    if (n > RHS_TABLE_MAX) return t;
+    t.n = n;
+    for (int q = 0; q < n; q++) {
+        const BatchInst<float>& I = b->h_tab32[q];
+        const RhsIn<float>& in = I.in[cur];
+        const Update<float>& up = I.up[s][cur];
+        RhsMember32& M = t.m[q];
+        M.base = I.g.base; M.P = (int)I.g.P; M.PS = (int)I.g.PS; M.mx = I.g.mx; M.my = I.g.my;
+        M.nbx = I.nbx; M.nby = I.nby; M.nonuniform_x = I.g.nonuniform_x;
+        M.use_prev = up.use_prev; M.fuse = up.fuse; M.vexp_is_one = up.ph.vexp_is_one;
+        for (int d = 0; d < 3; d++) { M.inv[d] = I.cf.inv[d]; M.inv2[d] = I.cf.inv2[d]; }
+        M.lam_mu = I.cf.lam_mu; M.ca = up.ca; M.cb = up.cb; M.f_vexp = up.ph.f_vexp; M.f_invRe = up.ph.f_invRe;
+        M.cvInv = up.ph.cvInv; M.Rgas = up.ph.Rgas;
+        M.xp = I.cf.xp; M.cvsx = I.cf.cvsx;
+        M.qa = in.qa; M.qb = in.qb; M.dil = in.dil;
+        const double* qi[5] = {up.qin.r, up.qin.u, up.qin.v, up.qin.w, up.qin.e};
+        double* qo[5] = {up.qout.r, up.qout.u, up.qout.v, up.qout.w, up.qout.e};
+        for (int f = 0; f < 5; f++) { M.qin[f] = qi[f]; M.qout[f] = qo[f]; M.rb[f] = up.rb[f]; }
+        M.spx = up.spx; M.spz = up.spz; M.rref = up.rref; M.uref = up.uref; M.vref = up.vref; M.wref = up.wref;
+        M.eref = up.eref;
+        M.nqa = up.dnext.qa; M.nqb = up.dnext.qb;
+        M.scal = I.scal;
+        t.unit_off[q + 1] = t.unit_off[q] + (long long)I.nbx * I.nby * I.g.mz;
+    }
+    return t;
 }
 
 int launch_stage(cns_batch* b, int s, int cur) {
@@ -202,10 +245,10 @@ int launch_stage(cns_batch* b, int s, int cur) {
     }
     if (f32)
         launch_batch_stage_fp32(b->S, b->V, grid, (const BatchInst<float>*)b->d_tab, b->d_ctl, cur, s, b->quirk,
-                                b->d_bar, b->d_err, b->stream);
+                                b->d_bar, b->d_err, b->d_cnt, rhs_table(b, s, cur), b->stream);
     else
         launch_batch_stage_fp64(b->S, b->V, grid, (const BatchInst<double>*)b->d_tab, b->d_ctl, cur, s, b->quirk,
-                                b->d_bar, b->d_err, b->stream);
+                                b->d_bar, b->d_err, b->d_cnt, RhsTable<double>{0}, b->stream);
     b->launches++;
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) {
@@ -322,6 +365,8 @@ int cns_batch_create(int device, int precision, int stencil_size, int stencil_vi
     if (e == cudaSuccess) e = cudaMalloc((void**)&b->d_bar, 2 * sizeof(unsigned));
     if (e == cudaSuccess) e = cudaMalloc((void**)&b->d_err, sizeof(int));
     if (e == cudaSuccess) e = cudaMemset(b->d_bar, 0, 2 * sizeof(unsigned));
+    if (e == cudaSuccess) e = cudaMalloc((void**)&b->d_cnt, 4 * sizeof(unsigned long long));
+    if (e == cudaSuccess) e = cudaMemset(b->d_cnt, 0, 4 * sizeof(unsigned long long));
     if (e == cudaSuccess) e = cudaMemset(b->d_err, 0, sizeof(int));
     if (e != cudaSuccess) {
         delete b;
@@ -504,6 +549,7 @@ int cns_batch_step(cns_batch* b, int nsteps) {
     if (err) {
         cudaMemset(b->d_err, 0, sizeof(int));
         cudaMemset(b->d_bar, 0, 2 * sizeof(unsigned));
+        cudaMemset(b->d_cnt, 0, 4 * sizeof(unsigned long long));
         return cns::set_error(CNS_ERR_TIMEOUT, "batch grid barrier gave up (bounded wait)");
     }
     for (auto& m : b->members) {

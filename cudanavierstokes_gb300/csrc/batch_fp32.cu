@@ -7,8 +7,9 @@ cudaError_t batch_occ_fp64(int S, int V, int* nb);
 
 namespace cns {
 void launch_batch_stage_fp32(int S, int V, dim3 grid, const BatchInst<float>* tab, const BatchCtl* ctl, int cur,
-                             int stage, int quirk, unsigned* bar, int* err, cudaStream_t s) {
-    batch_launch_dispatch<float>(S, V, grid, tab, ctl, cur, stage, quirk, bar, err, s);
+                             int stage, int quirk, unsigned* bar, int* err, unsigned long long* cnt, const RhsTable<float>& rt,
+                             cudaStream_t s) {
+    batch_launch_dispatch<float>(S, V, grid, tab, ctl, cur, stage, quirk, bar, err, cnt, rt, s);
 }
 void launch_batch_time_fp32(const BatchInst<float>* tab, const BatchCtl* ctl, cudaStream_t s) {
     batch_time_launch<float>(tab, ctl, s);

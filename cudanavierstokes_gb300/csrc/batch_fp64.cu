@@ -3,8 +3,9 @@
 
 namespace cns {
 void launch_batch_stage_fp64(int S, int V, dim3 grid, const BatchInst<double>* tab, const BatchCtl* ctl, int cur,
-                             int stage, int quirk, unsigned* bar, int* err, cudaStream_t s) {
-    batch_launch_dispatch<double>(S, V, grid, tab, ctl, cur, stage, quirk, bar, err, s);
+                             int stage, int quirk, unsigned* bar, int* err, unsigned long long* cnt, const RhsTable<double>& rt,
+                             cudaStream_t s) {
+    batch_launch_dispatch<double>(S, V, grid, tab, ctl, cur, stage, quirk, bar, err, cnt, rt, s);
 }
 void launch_batch_time_fp64(const BatchInst<double>* tab, const BatchCtl* ctl, cudaStream_t s) {
     batch_time_launch<double>(tab, ctl, s);

@@ -133,22 +133,127 @@ __device__ __forceinline__ void unit_point(const BatchInst<R>& I, long long lu, 
     j = by * 4 + ty;
 }
 
-// FP32: 5 blocks of 128 per SM (96 registers): the instance parameters come from the table in
-// global memory, not the constant bank, and at 7 blocks (72 registers) they spill 700 bytes a
-// thread (measured 1,095 vs 1,498 Mpoint-steps/s on the 48-member ensemble). FP64: 4 blocks.
-template <typename R, int S, int V>
-__global__ void __launch_bounds__(BATCH_THREADS, sizeof(R) == 4 ? 5 : 4)
+// FP32-RHS members' parameters of the RHS phase as a kernel argument (constant bank):
+// what the point body reads of the member's geometry, inverse spacings, packed stencil
+// inputs, Wray stage update and state recovery, for up to RHS_TABLE_MAX members. Read
+// through shared memory instead, these parameters took registers and issue slots in
+// every point (a one-member batch ran at 2,295 against 3,333 Mpoint-steps/s with them in
+// the constant bank); larger batches take that path (n = 0 in the table).
+constexpr int RHS_TABLE_MAX = 64;
+
+struct RhsMember32 {
+    long long base;
+    int P, PS, mx, my, nbx, nby, nonuniform_x, use_prev, fuse, vexp_is_one;
+    float inv[3], inv2[3], lam_mu, ca, cb, f_vexp, f_invRe;
+    double cvInv, Rgas;
+    const float* xp;
+    const float* cvsx;
+    const float4* qa;
+    const float4* qb;
+    const float* dil;
+    const double* qin[5];
+    double* qout[5];
+    float* rb[5];
+    const double *spx, *spz, *rref, *uref, *vref, *wref, *eref;
+    float4* nqa;
+    float4* nqb;
+    double* scal;
+};
+
+template <typename R>
+struct RhsTable {     // FP64 members keep the shared-memory path
+    int n;
+};
+template <>
+struct RhsTable<float> {
+    int n;                                     // members in the table; 0: use the shared-memory path
+    long long unit_off[RHS_TABLE_MAX + 1];     // point-unit prefix offsets (as BatchCtl's)
+    RhsMember32 m[RHS_TABLE_MAX];
+};
+
+// the RHS phase's point of member M: the standalone body (compile-time weights) on
+// geometry, coefficients, inputs and stage update assembled from the table entry
+template <int S, int V>
+__device__ __forceinline__ void rhs_point_member(const RhsMember32& M, int quirk, int i, int j, int k) {
+    Geom g{};
+    g.mx = M.mx; g.my = M.my; g.P = M.P; g.PS = M.PS; g.base = M.base; g.nonuniform_x = M.nonuniform_x;
+    CoefT<float> cf{};
+    for (int d = 0; d < 3; d++) { cf.inv[d] = M.inv[d]; cf.inv2[d] = M.inv2[d]; }
+    cf.lam_mu = M.lam_mu; cf.xp = M.xp; cf.cvsx = M.cvsx;
+    RhsIn<float> in{};
+    in.qa = M.qa; in.qb = M.qb; in.dil = M.dil;
+    Update<float> up{};
+    up.kind = ST_LS; up.ca = M.ca; up.cb = M.cb; up.use_prev = M.use_prev;
+    up.qin = StateIn{M.qin[0], M.qin[1], M.qin[2], M.qin[3], M.qin[4]};
+    up.qout = StateOut{M.qout[0], M.qout[1], M.qout[2], M.qout[3], M.qout[4]};
+    for (int q = 0; q < 5; q++) up.rb[q] = M.rb[q];
+    up.spx = M.spx; up.spz = M.spz; up.rref = M.rref; up.uref = M.uref; up.vref = M.vref; up.wref = M.wref;
+    up.eref = M.eref;
+    up.fuse = M.fuse; up.dnext.qa = M.nqa; up.dnext.qb = M.nqb;
+    up.ph.cvInv = M.cvInv; up.ph.Rgas = M.Rgas; up.ph.vexp_is_one = M.vexp_is_one; up.ph.f_vexp = M.f_vexp;
+    up.ph.f_invRe = M.f_invRe;
+    rhs_point<float, S, V, true>(g, cf, in, up, M.scal, quirk, i, j, k);
+}
+
+// Dynamic in-order scheduling of a phase's units: blocks take the next unit from a device
+// counter (one atomic per unit, issued while the block works on its current unit), so the
+// units in flight stay a compact window in unit order, as the hardware dispatches the
+// blocks of the standalone kernels, and faster blocks take more units. A block's units
+// increase, so its instance is found by a forward scan from the previous one.
+struct UnitQueue {
+    long long u;
+    int q, slot;
+    __device__ __forceinline__ UnitQueue(unsigned long long* c, long long* s_next) : u(0), q(0), slot(0) {
+        if (threadIdx.x == 0) s_next[0] = (long long)atomicAdd(c, 1ULL);
+        __syncthreads();
+        u = s_next[0];
+    }
+    // the instance of unit u (forward scan; units of one block only increase)
+    __device__ __forceinline__ void locate(const long long* off) {
+        while (u >= off[q + 1]) q++;
+    }
+};
+
+// FP32: 7 blocks of 128 per SM (72 registers); the RHS phase uses the packed body with
+// compile-time stencil weights, so a member's coefficients are six inverse spacings
+// instead of tables. FP64: 4 blocks.
+//
+// cnt[0..3]: the four phases' unit counters, zero at launch; each is reset by block 0 once
+// no block can take from it any more (after the barrier that ends its phase; the RHS
+// phase's counter at the start of the next launch, before its first barrier).
+// TBL: the RHS phase reads the members from the kernel-argument table (FP32, up to
+// RHS_TABLE_MAX members); otherwise through shared memory. Two instantiations, so that
+// neither path's registers constrain the other.
+template <typename R, int S, int V, bool TBL>
+__global__ void __launch_bounds__(BATCH_THREADS, sizeof(R) == 4 ? 7 : 4)
     k_batch_stage(const BatchInst<R>* __restrict__ tab, const BatchCtl* __restrict__ ctl, int cur, int stage,
-                  int quirk, unsigned* bar, int* err) {
+                  int quirk, unsigned* bar, int* err, unsigned long long* cnt,
+                  const __grid_constant__ RhsTable<R> rt) {
     const int n = ctl->n;
     if (n <= 0) return;
     const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
     const long long npu = ctl->unit_off[n], ngu = ctl->ghost_off[n];
     const unsigned nb = gridDim.x;
+    __shared__ long long s_next[2];
+    if (blockIdx.x == 0 && threadIdx.x == 0) cnt[3] = 0ULL;   // the previous launch's RHS counter
+
+    // one pass over the units of a phase: body(u, q) for every unit taken by this block
+    const auto sweep = [&](unsigned long long* c, const long long* off, long long total, auto&& body) {
+        UnitQueue w(c, s_next);
+        while (w.u < total) {
+            long long mine = 0;
+            if (threadIdx.x == 0) mine = (long long)atomicAdd(c, 1ULL);   // the next unit, in flight
+            w.locate(off);
+            body(w.u, w.q);
+            w.slot ^= 1;
+            if (threadIdx.x == 0) s_next[w.slot] = mine;
+            __syncthreads();
+            w.u = s_next[w.slot];
+        }
+    };
 
     // phase 1: ghost cells of the stencil inputs of the current state
-    for (long long u = blockIdx.x; u < ngu; u += gridDim.x) {
-        const int q = find_inst(ctl->ghost_off, n, u);
+    sweep(cnt + 0, ctl->ghost_off, ngu, [&](long long u, int q) {
         const BatchInst<R>& I = tab[q];
         const long long t = (u - ctl->ghost_off[q]) * BATCH_THREADS + threadIdx.x;
         if (t < ghost_count(I.g)) {
@@ -157,12 +262,12 @@ __global__ void __launch_bounds__(BATCH_THREADS, sizeof(R) == 4 ? 5 : 4)
                                      (R*)in.m, (float4*)in.qa, (float4*)in.qb};
             ghost_state_cell<R>(I.g, I.ph, f, I.scal, (int)t);
         }
-    }
+    });
     grid_barrier(bar, nb, err);
+    if (blockIdx.x == 0 && threadIdx.x == 0) cnt[0] = 0ULL;
     // phase 2: dilatation from the packed records (FP32-RHS: the RHS forms the nine gradients
     // itself) or the nine velocity gradients and the dilatation
-    for (long long u = blockIdx.x; u < npu; u += gridDim.x) {
-        const int q = find_inst(ctl->unit_off, n, u);
+    sweep(cnt + 1, ctl->unit_off, npu, [&](long long u, int q) {
         const BatchInst<R>& I = tab[q];
         int i, j, k;
         unit_point(I, u - ctl->unit_off[q], tx, ty, i, j, k);
@@ -177,42 +282,53 @@ __global__ void __launch_bounds__(BATCH_THREADS, sizeof(R) == 4 ? 5 : 4)
                 grad_point<R, V>(I.g, I.cf, in.u, in.v, in.w, go, i, j, k);
             }
         }
-    }
+    });
     grid_barrier(bar, nb, err);
+    if (blockIdx.x == 0 && threadIdx.x == 0) cnt[1] = 0ULL;
     // phase 3: dilatation ghosts
-    for (long long u = blockIdx.x; u < ngu; u += gridDim.x) {
-        const int q = find_inst(ctl->ghost_off, n, u);
+    sweep(cnt + 2, ctl->ghost_off, ngu, [&](long long u, int q) {
         const BatchInst<R>& I = tab[q];
         const long long t = (u - ctl->ghost_off[q]) * BATCH_THREADS + threadIdx.x;
         if (t < ghost_count(I.g)) ghost_scalar_cell<R>(I.g, (R*)I.in[cur].dil, (int)t);
-    }
+    });
     grid_barrier(bar, nb, err);
+    if (blockIdx.x == 0 && threadIdx.x == 0) cnt[2] = 0ULL;
     // phase 4: RHS + stage update into the other state buffer + that state's recovery, every
-    // neighbour from global memory (the standalone RHS kernel's point body). The unit's
-    // instance parameters (geometry, coefficients, inputs, stage update) are staged in
-    // shared memory when the instance changes: the point body reads them there instead of
-    // through the table in global memory.
+    // neighbour from global memory (the standalone RHS kernel's point body, compile-time
+    // weights). FP32 batches of up to RHS_TABLE_MAX members read a unit's member parameters
+    // from the kernel argument table; otherwise they are staged in shared memory when the
+    // member changes.
+    if constexpr (sizeof(R) == 4 && TBL) {
+        {
+            sweep(cnt + 3, rt.unit_off, npu, [&](long long u, int q) {
+                const RhsMember32& M = rt.m[q];
+                const long long lu = u - rt.unit_off[q];
+                const long long pl = (long long)M.nbx * M.nby;
+                const int k = (int)(lu / pl);
+                const int rr = (int)(lu - (long long)k * pl);
+                const int by = rr / M.nbx, bx = rr - by * M.nbx;
+                const int i = bx * 32 + tx, j = by * 4 + ty;
+                if (i < M.mx && j < M.my) rhs_point_member<S, V>(M, quirk, i, j, k);
+            });
+        }
+    } else {
     __shared__ StageParams<R> sp;
     int qs = -1;
-    for (long long u = blockIdx.x; u < npu; u += gridDim.x) {
-        const int q = find_inst(ctl->unit_off, n, u);
+    sweep(cnt + 3, ctl->unit_off, npu, [&](long long u, int q) {
         if (q != qs) {
             __syncthreads();   // the previous unit is done with sp
             stage_params_copy<R>(sp, tab[q], cur, stage);
             __syncthreads();
             qs = q;
         }
-        int i, j, k;
         const long long lu = u - ctl->unit_off[q];
-        {
-            const long long pl = (long long)sp.nbx * sp.nby;
-            k = (int)(lu / pl);
-            const int r = (int)(lu - (long long)k * pl);
-            const int by = r / sp.nbx, bx = r - by * sp.nbx;
-            i = bx * 32 + tx;
-            j = by * 4 + ty;
-        }
-        if (i < sp.g.mx && j < sp.g.my) rhs_point<R, S, V>(sp.g, sp.cf, sp.in, sp.up, sp.scal, quirk, i, j, k);
+        const long long pl = (long long)sp.nbx * sp.nby;
+        const int k = (int)(lu / pl);
+        const int rr = (int)(lu - (long long)k * pl);
+        const int by = rr / sp.nbx, bx = rr - by * sp.nbx;
+        const int i = bx * 32 + tx, j = by * 4 + ty;
+        if (i < sp.g.mx && j < sp.g.my) rhs_point<R, S, V, true>(sp.g, sp.cf, sp.in, sp.up, sp.scal, quirk, i, j, k);
+    });
     }
 }
 

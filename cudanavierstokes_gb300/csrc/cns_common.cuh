@@ -63,9 +63,30 @@ struct CoefT {
     R fq[3][5];      // 0.5  * c1S: split-form quadratic flux (rho u) weights
     R fc[3][5];      // 0.25 * c1S: split-form cubic flux (rho u phi) weights
     R lam_mu;        // lambda / mu = 1 / (Pr Ec)
+    R inv[3];        // inverse grid spacing of each direction (d_dx, d_dy, d_dz)
+    R inv2[3];       // their squares
     const R* xp;     // [mx]
     const R* cvsx;   // [(2V+1)*mx], index it*mx + i
 };
+
+// Central-difference weights of half-width K as compile-time constants (the same tables,
+// src/globals.h:69-95: fd1(K, k) = -coeffF[K-k], fd2(K, k) = coeffS[K-k]), for point bodies
+// that scale the weighted sums by the inverse spacings instead of reading premultiplied
+// tables. Standard central (Fornberg) weights of order 2K.
+__host__ __device__ constexpr float fd1(int K, int k) {
+    return K == 1 ? (k == 1 ? 1.0f / 2.0f : 0.0f)
+         : K == 2 ? (k == 1 ? 2.0f / 3.0f : k == 2 ? -1.0f / 12.0f : 0.0f)
+         : K == 3 ? (k == 1 ? 3.0f / 4.0f : k == 2 ? -3.0f / 20.0f : k == 3 ? 1.0f / 60.0f : 0.0f)
+         : (k == 1 ? 4.0f / 5.0f : k == 2 ? -1.0f / 5.0f : k == 3 ? 4.0f / 105.0f : k == 4 ? -1.0f / 280.0f : 0.0f);
+}
+__host__ __device__ constexpr float fd2(int K, int k) {
+    return K == 1 ? (k == 0 ? -2.0f : k == 1 ? 1.0f : 0.0f)
+         : K == 2 ? (k == 0 ? -5.0f / 2.0f : k == 1 ? 4.0f / 3.0f : k == 2 ? -1.0f / 12.0f : 0.0f)
+         : K == 3 ? (k == 0 ? -49.0f / 18.0f : k == 1 ? 3.0f / 2.0f : k == 2 ? -3.0f / 20.0f : k == 3 ? 1.0f / 90.0f
+                                                                                                   : 0.0f)
+         : (k == 0 ? -205.0f / 72.0f : k == 1 ? 8.0f / 5.0f : k == 2 ? -1.0f / 5.0f : k == 3 ? 8.0f / 315.0f
+                                                                                    : k == 4 ? -1.0f / 560.0f : 0.0f);
+}
 
 // perturbation of the bottom-wall u ghosts (src/perturbation.h:25-53)
 __device__ __forceinline__ bool wall_perturbation(const Phys& ph, double dy_inv, int j, int k, double time,

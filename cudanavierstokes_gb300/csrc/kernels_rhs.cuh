@@ -371,7 +371,14 @@ __device__ __forceinline__ void rhs_point_nb(const Geom& g, const CoefT<R>& cf, 
 // accumulated in the order of the FP64-mode body (centre term, then l ascending) with the
 // same expressions; the non-uniform x second derivative adds the pair (l, -l) per l.
 // ---------------------------------------------------------------------------------
-template <int S, int V, int DIR>
+//
+// CW (compile-time weights): the sums use the central-difference weights as immediates and
+// are scaled by the direction's inverse spacing (or its square) afterwards; the flux sums
+// carry neither 1/2, 1/4 nor 1/dx, which the final combination applies. The batched stage
+// kernel uses this form: its members' coefficients would otherwise come through shared
+// memory and occupy registers. The standalone kernel reads the premultiplied tables from
+// its launch parameters (constant bank operands).
+template <int S, int V, int DIR, bool CW>
 __device__ __forceinline__ void rhs_dir_packed(const Geom& g, const CoefT<float>& cf, const RhsIn<float>& in, int c,
                                                int st, int i, float (&Gr)[9], float m0, float m3, float u0, float v0,
                                                float w0, float r0, float h0, float T0, float (&acc)[5],
@@ -384,6 +391,11 @@ __device__ __forceinline__ void rhs_dir_packed(const Geom& g, const CoefT<float>
     const float* c2V = cf.c2V[DIR];
     const float* fq = cf.fq[DIR];
     const float* fcb = cf.fc[DIR];
+    const auto w1V = [&](int l) { if constexpr (CW) return fd1(V, l); else return c1V[l]; };
+    const auto w1S = [&](int l) { if constexpr (CW) return fd1(S, l); else return c1S[l]; };
+    const auto w2V = [&](int l) { if constexpr (CW) return fd2(V, l); else return c2V[l]; };
+    const auto wq = [&](int l) { if constexpr (CW) return fd1(S, l); else return fq[l]; };
+    const auto wc = [&](int l) { if constexpr (CW) return fd1(S, l); else return fcb[l]; };
     const float un = DIR == 0 ? u0 : (DIR == 1 ? v0 : w0);
 
     float gu = 0.f, gv = 0.f, gw = 0.f, dmu = 0.f, dT = 0.f, dth = 0.f, dp = 0.f;
@@ -392,10 +404,10 @@ __device__ __forceinline__ void rhs_dir_packed(const Geom& g, const CoefT<float>
         const float cw = __ldg(cf.cvsx + V * g.mx + i);
         d2uu = cw * u0; d2vv = cw * v0; d2ww = cw * w0; d2tt = cw * T0;
     } else {
-        d2uu = c2V[0] * u0; d2vv = c2V[0] * v0; d2ww = c2V[0] * w0; d2tt = c2V[0] * T0;
+        d2uu = w2V(0) * u0; d2vv = w2V(0) * v0; d2ww = w2V(0) * w0; d2tt = w2V(0) * T0;
     }
-    float sq = 0.f, fu = nux ? 0.f : acc[1], fv = nux ? 0.f : acc[2], fw = nux ? 0.f : acc[3],
-          fe = nux ? 0.f : acc[4];
+    float sq = 0.f, fu = (nux || CW) ? 0.f : acc[1], fv = (nux || CW) ? 0.f : acc[2],
+          fw = (nux || CW) ? 0.f : acc[3], fe = (nux || CW) ? 0.f : acc[4];
 #pragma unroll
     for (int l = 1; l <= S; l++) {
         const float4 Ap = __ldg(in.qa + c + l * st), Am = __ldg(in.qa + c - l * st);
@@ -403,13 +415,13 @@ __device__ __forceinline__ void rhs_dir_packed(const Geom& g, const CoefT<float>
         if (l <= V) {
             const float thp = __ldg(in.dil + c + l * st), thm = __ldg(in.dil + c - l * st);
             if (l == 1) {
-                gu = c1V[1] * (Ap.y - Am.y); gv = c1V[1] * (Ap.z - Am.z); gw = c1V[1] * (Ap.w - Am.w);
-                dmu = c1V[1] * (Bp.w - Bm.w); dT = c1V[1] * (Bp.x - Bm.x); dth = c1V[1] * (thp - thm);
+                gu = w1V(1) * (Ap.y - Am.y); gv = w1V(1) * (Ap.z - Am.z); gw = w1V(1) * (Ap.w - Am.w);
+                dmu = w1V(1) * (Bp.w - Bm.w); dT = w1V(1) * (Bp.x - Bm.x); dth = w1V(1) * (thp - thm);
             } else {
-                gu = fma(c1V[l], Ap.y - Am.y, gu); gv = fma(c1V[l], Ap.z - Am.z, gv);
-                gw = fma(c1V[l], Ap.w - Am.w, gw);
-                dmu = fma(c1V[l], Bp.w - Bm.w, dmu); dT = fma(c1V[l], Bp.x - Bm.x, dT);
-                dth = fma(c1V[l], thp - thm, dth);
+                gu = fma(w1V(l), Ap.y - Am.y, gu); gv = fma(w1V(l), Ap.z - Am.z, gv);
+                gw = fma(w1V(l), Ap.w - Am.w, gw);
+                dmu = fma(w1V(l), Bp.w - Bm.w, dmu); dT = fma(w1V(l), Bp.x - Bm.x, dT);
+                dth = fma(w1V(l), thp - thm, dth);
             }
             if (nux) {
                 const float cp = __ldg(cf.cvsx + (V + l) * g.mx + i), cm = __ldg(cf.cvsx + (V - l) * g.mx + i);
@@ -418,58 +430,74 @@ __device__ __forceinline__ void rhs_dir_packed(const Geom& g, const CoefT<float>
                 d2ww = fma(cp, Ap.w, fma(cm, Am.w, d2ww));
                 d2tt = fma(cp, Bp.x, fma(cm, Bm.x, d2tt));
             } else {
-                d2uu = fma(c2V[l], Ap.y + Am.y, d2uu);
-                d2vv = fma(c2V[l], Ap.z + Am.z, d2vv);
-                d2ww = fma(c2V[l], Ap.w + Am.w, d2ww);
-                d2tt = fma(c2V[l], Bp.x + Bm.x, d2tt);
+                d2uu = fma(w2V(l), Ap.y + Am.y, d2uu);
+                d2vv = fma(w2V(l), Ap.z + Am.z, d2vv);
+                d2ww = fma(w2V(l), Ap.w + Am.w, d2ww);
+                d2tt = fma(w2V(l), Bp.x + Bm.x, d2tt);
             }
         }
-        dp = l == 1 ? c1S[1] * (Bp.y - Bm.y) : fma(c1S[l], Bp.y - Bm.y, dp);
+        dp = l == 1 ? w1S(1) * (Bp.y - Bm.y) : fma(w1S(l), Bp.y - Bm.y, dp);
         // telescoped split-form fluxes (rhs_direction: a_l Q+- shared by the cubic fluxes)
         const float gm = DIR == 0 ? Am.y : (DIR == 1 ? Am.z : Am.w);
         const float gp = DIR == 0 ? Ap.y : (DIR == 1 ? Ap.z : Ap.w);
         const float Qm = (Am.x + r0) * (gm + un);
         const float Qp = (r0 + Ap.x) * (un + gp);
-        sq = fma(fq[l], Qm - Qp, sq);
-        const float am = fcb[l] * Qm, ap = fcb[l] * Qp;
+        sq = fma(wq(l), Qm - Qp, sq);
+        const float am = wc(l) * Qm, ap = wc(l) * Qp;
         fu = fma(am, Am.y, fma(-ap, Ap.y, fu));
         fv = fma(am, Am.z, fma(-ap, Ap.z, fv));
         fw = fma(am, Am.w, fma(-ap, Ap.w, fw));
         fe = fma(am, Bm.z, fma(-ap, Bp.z, fe));
     }
-    if (nux) { gu *= xpi; gv *= xpi; gw *= xpi; }
+    // first derivatives: x' on a non-uniform x; with CW also the inverse spacing
+    const float s1 = CW ? cf.inv[DIR] * xpi : xpi;
+    if (nux || CW) { gu *= s1; gv *= s1; gw *= s1; }
     Gr[3 * DIR + 0] = gu; Gr[3 * DIR + 1] = gv; Gr[3 * DIR + 2] = gw;
-    dmu *= xpi;
+    if (CW && !nux) {
+        const float s2 = cf.inv2[DIR];
+        d2uu *= s2; d2vv *= s2; d2ww *= s2; d2tt *= s2;
+    }
+    dmu *= s1;
     dmu_dir = dmu;
     W[0] = fma(d2uu, m0, W[0]);
     W[1] = fma(d2vv, m0, W[1]);
     W[2] = fma(d2ww, m0, W[2]);
     // heat conduction (lambda / mu)(mu d2T + dmu dT), the ratio applied once per point
-    dT *= xpi;
+    dT *= s1;
     cond = fma(d2tt, m0, cond);
     cond = fma(dT, dmu, cond);
-    dth *= xpi;
-    dp *= xpi;
+    dth *= s1;
+    dp *= s1;
     W[DIR] = fma(m3, dth, W[DIR]);
-    const float half = 0.5f * sq;
-    fu = fma(u0, half, fu);
-    fv = fma(v0, half, fv);
-    fw = fma(w0, half, fw);
-    fe = fma(h0, half, fe);
-    const float fr = nux ? sq : acc[0] + sq;
-    if (nux) {
-        acc[0] = fma(xpi, fr, acc[0]);
-        acc[1] = fma(xpi, fu, acc[1]);
-        acc[2] = fma(xpi, fv, acc[2]);
-        acc[3] = fma(xpi, fw, acc[3]);
-        acc[4] = fma(xpi, fe, acc[4]);
+    if constexpr (CW) {
+        // fluxes: mass c/dx * sq with c = 1/2, the cubic ones c/dx (f + phi_0 sq) with c = 1/4
+        const float q2 = 0.5f * s1, q4 = 0.25f * s1;
+        acc[0] = fma(q2, sq, acc[0]);
+        acc[1] = fma(q4, fma(u0, sq, fu), acc[1]);
+        acc[2] = fma(q4, fma(v0, sq, fv), acc[2]);
+        acc[3] = fma(q4, fma(w0, sq, fw), acc[3]);
+        acc[4] = fma(q4, fma(h0, sq, fe), acc[4]);
     } else {
-        acc[0] = fr; acc[1] = fu; acc[2] = fv; acc[3] = fw; acc[4] = fe;
+        const float half = 0.5f * sq;
+        fu = fma(u0, half, fu);
+        fv = fma(v0, half, fv);
+        fw = fma(w0, half, fw);
+        fe = fma(h0, half, fe);
+        const float fr = nux ? sq : acc[0] + sq;
+        if (nux) {
+            acc[0] = fma(xpi, fr, acc[0]);
+            acc[1] = fma(xpi, fu, acc[1]);
+            acc[2] = fma(xpi, fv, acc[2]);
+            acc[3] = fma(xpi, fw, acc[3]);
+            acc[4] = fma(xpi, fe, acc[4]);
+        } else {
+            acc[0] = fr; acc[1] = fu; acc[2] = fv; acc[3] = fw; acc[4] = fe;
+        }
     }
     acc[1 + DIR] -= dp;
 }
 
-template <int S, int V>
+template <int S, int V, bool CW>
 __device__ __forceinline__ void rhs_point_packed(const Geom& g, const CoefT<float>& cf, const RhsIn<float>& in,
                                                  const Update<float>& up, double* __restrict__ scal, int quirk, int i,
                                                  int j, int k) {
@@ -484,9 +512,10 @@ __device__ __forceinline__ void rhs_point_packed(const Geom& g, const CoefT<floa
     float W[3] = {0, 0, 0};
     float diss = 0, cond = 0;
     float dmu[3];
-    rhs_dir_packed<S, V, 0>(g, cf, in, c, 1, i, Gr, m0, m3, u0, v0, w0, r0, h0, T0, acc, W, cond, dmu[0]);
-    rhs_dir_packed<S, V, 1>(g, cf, in, c, (int)g.P, i, Gr, m0, m3, u0, v0, w0, r0, h0, T0, acc, W, cond, dmu[1]);
-    rhs_dir_packed<S, V, 2>(g, cf, in, c, (int)g.PS, i, Gr, m0, m3, u0, v0, w0, r0, h0, T0, acc, W, cond, dmu[2]);
+    rhs_dir_packed<S, V, 0, CW>(g, cf, in, c, 1, i, Gr, m0, m3, u0, v0, w0, r0, h0, T0, acc, W, cond, dmu[0]);
+    rhs_dir_packed<S, V, 1, CW>(g, cf, in, c, (int)g.P, i, Gr, m0, m3, u0, v0, w0, r0, h0, T0, acc, W, cond, dmu[1]);
+    rhs_dir_packed<S, V, 2, CW>(g, cf, in, c, (int)g.PS, i, Gr, m0, m3, u0, v0, w0, r0, h0, T0, acc, W, cond,
+                                dmu[2]);
     // stress rows, dissipation and grad(mu) . s of every direction, now that all nine
     // gradients are known (y: tau_yz dv/dz with the quirk, src/cuda_rhs.cu:175)
 #pragma unroll
@@ -511,11 +540,12 @@ __device__ __forceinline__ void rhs_point_packed(const Geom& g, const CoefT<floa
 }
 
 // RHS + stage update of one interior point (i, j, k), every neighbour from global memory
-template <typename R, int S, int V>
+// (CW: the FP32 body with compile-time weights, see rhs_dir_packed)
+template <typename R, int S, int V, bool CW = false>
 __device__ __forceinline__ void rhs_point(const Geom& g, const CoefT<R>& cf, const RhsIn<R>& in, const Update<R>& up,
                                           double* __restrict__ scal, int quirk, int i, int j, int k) {
     if constexpr (sizeof(R) == 4) {
-        rhs_point_packed<S, V>(g, cf, in, up, scal, quirk, i, j, k);
+        rhs_point_packed<S, V, CW>(g, cf, in, up, scal, quirk, i, j, k);
     } else {
         const int c = (int)g.at(i, j, k);
         const R th0 = ld(in.dil, c), m0 = ld(in.m, c);

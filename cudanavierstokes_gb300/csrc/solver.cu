@@ -485,6 +485,11 @@ int cns_create(const cns_params* pin, int device, cns_solver** out) {
     // lambda = mu / (Pr Ec)  (calcState, src/cuda_main.cu:218-242)
     h->cf64.lam_mu = 1.0 / (p.Pr * ph.Ec);
     h->cf32.lam_mu = (float)h->cf64.lam_mu;
+    const double inv[3] = {h->hg.dx, h->hg.dy, h->hg.dz}, inv2[3] = {h->hg.d2x, h->hg.d2y, h->hg.d2z};
+    for (int d = 0; d < 3; d++) {
+        h->cf64.inv[d] = inv[d]; h->cf64.inv2[d] = inv2[d];
+        h->cf32.inv[d] = (float)inv[d]; h->cf32.inv2[d] = (float)inv2[d];
+    }
 
     CK(cudaStreamCreateWithFlags(&h->own_stream, cudaStreamNonBlocking));
     h->stream = h->own_stream;

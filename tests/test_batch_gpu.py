@@ -47,9 +47,12 @@ def test_batch_matches_standalone_solvers(gpu_lib, prec, mode):
         errs = state_errors(bt.fields(mid), s.copy_field_out())
         assert max(errs) <= tol, (mid, errs)
         lb = bt.logs(mid, n)
-        np.testing.assert_allclose(lb["time"], lg["time"], rtol=1e-12)
+        # FP32 RHS: the persistent kernel scales compile-time stencil weights by the spacing,
+        # the standalone kernel uses premultiplied weights, so they agree to FP32 rounding
+        # and the time steps (from the state) to well within the state tolerance
+        np.testing.assert_allclose(lb["time"], lg["time"], rtol=1e-12 if prec == PREC_FP64 else tol)
         has = ~np.isnan(lg["par1"])
-        np.testing.assert_allclose(lb["par1"][has], lg["par1"][has], rtol=1e-10)
+        np.testing.assert_allclose(lb["par1"][has], lg["par1"][has], rtol=1e-10 if prec == PREC_FP64 else tol)
         assert bt.steps_done(mid) == n
 
 
