@@ -146,19 +146,18 @@ __device__ __forceinline__ double to_d(R x) {
     if constexpr (sizeof(R) == 4) return f2d(x); else return x;
 }
 
-// Reciprocal of a double: FP32 seed refined by two Newton steps (error squared each
-// step: 2^-24 -> 2^-48 -> 2^-96 before the final rounding), cheaper than the IEEE division
-// on the FP64 pipe. The seed needs x and 1/x to be FP32 normals, so magnitudes outside
-// [2^-125, 2^125) (and zero, infinity, NaN) take the IEEE division; densities never do.
-// A GPU self test (cns_selftest_rcp) bounds it at one ulp of 1.0 / x.
+// Reciprocal of a double from an FP32 seed r0 (|e| <= ~2^-23 with e = 1 - x r0):
+// 1/x = r0 / (1 - e) = r0 (1 + e + e^2 + ...), taken to e^2 (cubic convergence, truncation
+// ~2^-69, below the final rounding) in three fused multiply-adds, cheaper than the IEEE
+// division on the FP64 pipe. The seed needs x and 1/x to be FP32 normals, so magnitudes
+// outside [2^-125, 2^125) (and zero, infinity, NaN) take the IEEE division; densities never
+// do. A GPU self test (cns_selftest_rcp) bounds it at one ulp of 1.0 / x.
 __device__ __forceinline__ double rcp_nr(double x) {
     const unsigned ah = (unsigned)__double2hiint(x) & 0x7fffffffu;
     if (ah - 0x38200000u >= 0x47c00000u - 0x38200000u) return 1.0 / x;   // |x| outside [2^-125, 2^125)
-    double r = f2d(__frcp_rn(d2f(x)));
-    double e = fma(-x, r, 1.0);
-    r = fma(r, e, r);
-    e = fma(-x, r, 1.0);
-    return fma(r, e, r);
+    const double r = f2d(__frcp_rn(d2f(x)));
+    const double e = fma(-x, r, 1.0);
+    return fma(r, fma(e, e, e), r);
 }
 
 // x^a in FP64 for the viscosity law mu ~ T^a, as exp(a ln x) with

@@ -18,11 +18,14 @@ namespace cns {
 template <typename R>
 __device__ __forceinline__ void state_store(const Phys& ph, const DerivedOut<R>& o, double* scal, long long c,
                                             double rr, double inv, double uu, double vv, double ww, double ee) {
-    const double en = ee * inv - 0.5 * (uu * uu + vv * vv + ww * ww);
-    const double T = ph.cvInv * en;
-    const double pr = rr * ph.Rgas * T;
-    const double hh = (ee + pr) * inv;
     if constexpr (sizeof(R) == 4) {
+        // FP32-RHS: the same recovery with R T shared by p = rho (R T) and H = E/rho + R T
+        // (= (rhoE + p)/rho), one FP64 operation fewer on the pipe this mode is short of
+        const double er = ee * inv;
+        const double T = ph.cvInv * fma(-0.5, uu * uu + vv * vv + ww * ww, er);
+        const double RT = ph.Rgas * T;
+        const double pr = rr * RT;
+        const double hh = er + RT;
         const float Tf = d2f(T);
         const float suth = ph.vexp_is_one ? Tf : powf(Tf, ph.f_vexp);
         const float rf = d2f(rr);
@@ -31,6 +34,10 @@ __device__ __forceinline__ void state_store(const Phys& ph, const DerivedOut<R>&
         // the positivity test on the FP32 roundings keeps it off the FP64 pipe
         if (!(Tf > 0.f) || !(rf > 0.f)) scal[SC_NONFINITE] = 1.0;   // racy flag write, any writer is fine
     } else {
+        const double en = ee * inv - 0.5 * (uu * uu + vv * vv + ww * ww);
+        const double T = ph.cvInv * en;
+        const double pr = rr * ph.Rgas * T;
+        const double hh = (ee + pr) * inv;
         o.t[c] = T;
         o.p[c] = pr;
         o.h[c] = hh;
