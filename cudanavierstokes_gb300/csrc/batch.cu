@@ -223,9 +223,9 @@ RhsTable<float> rhs_table(const cns_batch* b, int s, int cur) {
         M.cvInv = up.ph.cvInv; M.Rgas = up.ph.Rgas;
         M.xp = I.cf.xp; M.cvsx = I.cf.cvsx;
         M.qa = in.qa; M.qb = in.qb; M.dil = in.dil;
-        const double* qi[5] = {up.qin.r, up.qin.u, up.qin.v, up.qin.w, up.qin.e};
-        double* qo[5] = {up.qout.r, up.qout.u, up.qout.v, up.qout.w, up.qout.e};
-        for (int f = 0; f < 5; f++) { M.qin[f] = qi[f]; M.qout[f] = qo[f]; M.rb[f] = up.rb[f]; }
+        // the state buffers and the RK register are single blocks with field stride nalloc
+        M.fstride = b->members[q].h->nalloc;
+        M.qin = up.qin.r; M.qout = up.qout.r; M.rb = up.rb[0];
         M.spx = up.spx; M.spz = up.spz; M.rref = up.rref; M.uref = up.uref; M.vref = up.vref; M.wref = up.wref;
         M.eref = up.eref;
         M.nqa = up.dnext.qa; M.nqb = up.dnext.qb;

@@ -151,9 +151,10 @@ struct RhsMember32 {
     const float4* qa;
     const float4* qb;
     const float* dil;
-    const double* qin[5];
-    double* qout[5];
-    float* rb[5];
+    long long fstride;    // elements between the fields of a state buffer / the RK register
+    const double* qin;    // rho of the stage's input state; u, v, w, rhoE follow at fstride
+    double* qout;         // the same of the output state
+    float* rb;            // the RK register's first field
     const double *spx, *spz, *rref, *uref, *vref, *wref, *eref;
     float4* nqa;
     float4* nqb;
@@ -184,9 +185,10 @@ __device__ __forceinline__ void rhs_point_member(const RhsMember32& M, int quirk
     in.qa = M.qa; in.qb = M.qb; in.dil = M.dil;
     Update<float> up{};
     up.kind = ST_LS; up.ca = M.ca; up.cb = M.cb; up.use_prev = M.use_prev;
-    up.qin = StateIn{M.qin[0], M.qin[1], M.qin[2], M.qin[3], M.qin[4]};
-    up.qout = StateOut{M.qout[0], M.qout[1], M.qout[2], M.qout[3], M.qout[4]};
-    for (int q = 0; q < 5; q++) up.rb[q] = M.rb[q];
+    const long long fs = M.fstride;
+    up.qin = StateIn{M.qin, M.qin + fs, M.qin + 2 * fs, M.qin + 3 * fs, M.qin + 4 * fs};
+    up.qout = StateOut{M.qout, M.qout + fs, M.qout + 2 * fs, M.qout + 3 * fs, M.qout + 4 * fs};
+    for (int q = 0; q < 5; q++) up.rb[q] = M.rb + q * fs;
     up.spx = M.spx; up.spz = M.spz; up.rref = M.rref; up.uref = M.uref; up.vref = M.vref; up.wref = M.wref;
     up.eref = M.eref;
     up.fuse = M.fuse; up.dnext.qa = M.nqa; up.dnext.qb = M.nqb;

@@ -497,7 +497,7 @@ int cns_create(const cns_params* pin, int device, cns_solver** out) {
     const size_t rs = h->rsz;
     const size_t N = (size_t)p.mx * p.my * p.mz;
     for (int b = 0; b < 2 && !rc; b++)
-        for (int f = 0; f < 5 && !rc; f++) rc = h->alloc_field((void**)&h->q[b][f], 8);
+        rc = h->alloc_fields((void**)h->q[b], 5, 8);   // rho, u, v, w, rhoE of buffer b in one block
     for (int b = 0; b < 2; b++) {
         if (h->fp32)   // packed FP32 records (rho, u, v, w) and (T, p, H, mu)
             for (int f = 0; f < 2 && !rc; f++) rc = h->alloc_field(&h->der[b][f], sizeof(float4));
@@ -507,7 +507,7 @@ int cns_create(const cns_params* pin, int device, cns_solver** out) {
     if (!rc) rc = h->alloc_field(&h->dil, rs);
     if (!h->fp32)   // FP32-RHS: the RHS kernel forms the velocity gradients itself
         for (int f = 0; f < 9 && !rc; f++) rc = h->alloc_field(&h->grad[f], rs);
-    for (int f = 0; f < 5 && !rc; f++) rc = h->alloc_field(&h->rb[f], rs);
+    if (!rc) rc = h->alloc_fields(h->rb, 5, rs);
     if (!rc && p.scheme != CNS_RK3_LOWSTORAGE) {
         for (int f = 0; f < 5 && !rc; f++) rc = h->alloc_field(&h->k2[f], rs);
         for (int f = 0; f < 5 && !rc; f++) rc = h->alloc_field((void**)&h->q0[f], 8);

@@ -84,6 +84,21 @@ struct cns_solver {
         *ptr = (T*)p0;
         return CNS_OK;
     }
+    // nf fields of esz bytes in one allocation, field f at ptr[f] = base + f * nalloc elements
+    // (a state buffer or an RK register as one block: kernels that take many fields can
+    // address them from one base pointer and the field stride nalloc)
+    int alloc_fields(void** ptr, int nf, size_t esz) {
+        void* p0 = nullptr;
+        cudaError_t e = cudaMalloc(&p0, (size_t)nalloc * esz * nf);
+        if (e != cudaSuccess) {
+            cudaGetLastError();
+            return cns::set_error(CNS_ERR_OOM, "cudaMalloc of a field group failed");
+        }
+        allocs.push_back(p0);
+        bytes += (int64_t)((size_t)nalloc * esz * nf);
+        for (int f = 0; f < nf; f++) ptr[f] = (char*)p0 + (size_t)f * nalloc * esz;
+        return CNS_OK;
+    }
     int alloc_field(void** ptr, size_t esz) {
         void* p0 = nullptr;
         cudaError_t e = cudaMalloc(&p0, (size_t)nalloc * esz);
