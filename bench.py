@@ -16,8 +16,10 @@ path is not sharded across GPUs, each rank advances its own channel).
   cpu_baseline  the CPU oracle (the reference's algorithm restated, OpenMP) on the host
               cores, on the same full channel (whole RK3 steps for ~12 s)
   fp32_rhs    the same workload with the RHS in FP32 (state/accumulation FP64)
-  batched     48 Taylor-Green boxes of uneven size (seeded), FP32 RHS / FP64 state, one
-              persistent launch per RK stage for the whole ensemble, graph replay, autotuned
+  batched     48 Taylor-Green boxes of uneven size (seeded), FP32 RHS / FP64 state, in the
+              execution mode the autotuner picks (one persistent launch per RK stage for the
+              whole ensemble, or every member's step graph on concurrent streams), graph
+              replay; the other mode is timed beside it
   serving     Poisson-arrival "advance N steps" requests (Taylor-Green 32^3-192^3 and
               64x48x64 channels, N in [50, 500]) under a 150 GB budget: p50/p99 latency and
               aggregate Mpoint-steps/s per arrival rate, 100 requests per rate, rates swept
@@ -254,6 +256,12 @@ def run_batched(args, stream_ptr, members=48, mode_req="tuned", with_other=True)
     oms, _ = timed()
     out["other_mode"] = {"mode": names[other], "value": pts * args.steps / (oms * 1e-3) / 1e6,
                          "ms_per_step": oms / args.steps}
+    if mode == 1:
+        out["why_mode"] = ("the persistent kernel runs the same point bodies, but a member's parameters reach "
+                           "them from a kernel-argument table indexed by member (registers and ~30 spill loads "
+                           "per point in the RHS phase) instead of as constant-bank operands, with compile-time "
+                           "stencil weights scaled by the spacings (+7 %) and point-per-thread theta; the "
+                           "concurrent mode keeps the standalone kernels (profiles/batch_stage_persistent_fp32.md)")
     if other == 0:
         out["other_mode"]["launch_shape"] = {"threads": 128, "blocks_per_sm": bt.shape()[1]}
     bt.close()
