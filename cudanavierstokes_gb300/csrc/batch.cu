@@ -230,7 +230,16 @@ RhsTable<float> rhs_table(const cns_batch* b, int s, int cur) {
         M.eref = up.eref;
         M.nqa = up.dnext.qa; M.nqb = up.dnext.qb;
         M.scal = I.scal;
+        M.G = I.g.G; M.mz = I.g.mz; M.xbc = I.g.xbc; M.zbl = I.g.zbl; M.dy = I.g.dy;
+        M.perturbed = I.ph.perturbed; M.pert_kc = I.ph.pert_kc; M.pert_lp = I.ph.pert_lp;
+        M.twall_top = I.ph.twall_top; M.twall_bot = I.ph.twall_bot; M.hcoef = I.ph.hcoef; M.invRe = I.ph.invRe;
+        M.vexp = I.ph.vexp;
+        M.pert_amp1 = I.ph.pert_amp1; M.pert_amp2 = I.ph.pert_amp2; M.pert_omega1 = I.ph.pert_omega1;
+        M.pert_omega2 = I.ph.pert_omega2; M.pert_lambda = I.ph.pert_lambda;
+        for (int d = 0; d < 3; d++)
+            for (int l = 0; l < 5; l++) M.c1V[d][l] = I.cf.c1V[d][l];
         t.unit_off[q + 1] = t.unit_off[q] + (long long)I.nbx * I.nby * I.g.mz;
+        t.ghost_off[q + 1] = t.ghost_off[q] + (ghost_count(I.g) + BATCH_THREADS - 1) / BATCH_THREADS;
     }
     return t;
 }

@@ -133,9 +133,9 @@ __device__ __forceinline__ void unit_point(const BatchInst<R>& I, long long lu, 
     j = by * 4 + ty;
 }
 
-// FP32-RHS members' parameters of the RHS phase as a kernel argument (constant bank):
-// what the point body reads of the member's geometry, inverse spacings, packed stencil
-// inputs, Wray stage update and state recovery, for up to RHS_TABLE_MAX members. Read
+// FP32-RHS members' parameters as a kernel argument (constant bank): what the four phases'
+// point bodies read of the member's geometry, inverse spacings, boundary constants, packed
+// stencil inputs, Wray stage update and state recovery, for up to RHS_TABLE_MAX members. Read
 // through shared memory instead, these parameters took registers and issue slots in
 // every point (a one-member batch ran at 2,295 against 3,333 Mpoint-steps/s with them in
 // the constant bank); larger batches take that path (n = 0 in the table).
@@ -159,6 +159,11 @@ struct RhsMember32 {
     float4* nqa;
     float4* nqb;
     double* scal;
+    // the ghost and theta phases: ghost geometry, boundary constants, theta weights
+    int G, mz, xbc, zbl, perturbed, pert_kc, pert_lp;
+    double twall_top, twall_bot, hcoef, invRe, vexp, dy;
+    double pert_amp1, pert_amp2, pert_omega1, pert_omega2, pert_lambda;
+    float c1V[3][5];
 };
 
 template <typename R>
@@ -169,8 +174,27 @@ template <>
 struct RhsTable<float> {
     int n;                                     // members in the table; 0: use the shared-memory path
     long long unit_off[RHS_TABLE_MAX + 1];     // point-unit prefix offsets (as BatchCtl's)
+    long long ghost_off[RHS_TABLE_MAX + 1];    // ghost-unit prefix offsets
     RhsMember32 m[RHS_TABLE_MAX];
 };
+// kernel arguments are limited to 32,764 bytes; the stage kernel's others take < 100
+static_assert(sizeof(RhsTable<float>) <= 32600, "the member table must fit the kernel-argument space");
+
+// a member's geometry and boundary constants for the ghost and theta phases
+__device__ __forceinline__ Geom member_geom(const RhsMember32& M) {
+    Geom g{};
+    g.mx = M.mx; g.my = M.my; g.mz = M.mz; g.G = M.G; g.P = M.P; g.PS = M.PS; g.base = M.base;
+    g.xbc = M.xbc; g.zbl = M.zbl; g.nonuniform_x = M.nonuniform_x; g.dy = M.dy;
+    return g;
+}
+__device__ __forceinline__ Phys member_phys(const RhsMember32& M) {
+    Phys ph{};
+    ph.Rgas = M.Rgas; ph.invRe = M.invRe; ph.hcoef = M.hcoef; ph.vexp = M.vexp; ph.vexp_is_one = M.vexp_is_one;
+    ph.twall_top = M.twall_top; ph.twall_bot = M.twall_bot; ph.perturbed = M.perturbed;
+    ph.pert_kc = M.pert_kc; ph.pert_lp = M.pert_lp; ph.pert_amp1 = M.pert_amp1; ph.pert_amp2 = M.pert_amp2;
+    ph.pert_omega1 = M.pert_omega1; ph.pert_omega2 = M.pert_omega2; ph.pert_lambda = M.pert_lambda;
+    return ph;
+}
 
 // the RHS phase's point of member M: the standalone body (compile-time weights) on
 // geometry, coefficients, inputs and stage update assembled from the table entry
@@ -254,6 +278,71 @@ __global__ void __launch_bounds__(BATCH_THREADS, sizeof(R) == 4 ? 7 : 4)
         }
     };
 
+    if constexpr (sizeof(R) == 4 && TBL) {
+        // members in outer loops: q is a loop counter, the same in every thread, and a
+        // member's parameters come from the kernel-argument table
+        const auto sweep_m = [&](unsigned long long* c, const long long* off, auto&& body) {
+            UnitQueue w(c, s_next);
+            for (int q = 0; q < rt.n; q++) {
+                const RhsMember32& M = rt.m[q];
+                while (w.u < off[q + 1]) {
+                    long long mine = 0;
+                    if (threadIdx.x == 0) mine = (long long)atomicAdd(c, 1ULL);   // the next unit, in flight
+                    body(M, w.u - off[q]);
+                    w.slot ^= 1;
+                    if (threadIdx.x == 0) s_next[w.slot] = mine;
+                    __syncthreads();
+                    w.u = s_next[w.slot];
+                }
+            }
+        };
+        const auto unit_ijk = [&](const RhsMember32& M, long long lu, int& i, int& j, int& k) {
+            const long long pl = (long long)M.nbx * M.nby;
+            k = (int)(lu / pl);
+            const int rr = (int)(lu - (long long)k * pl);
+            const int by = rr / M.nbx, bx = rr - by * M.nbx;
+            i = bx * 32 + tx;
+            j = by * 4 + ty;
+        };
+        // phase 1: ghost cells of the stencil inputs of the current state
+        sweep_m(cnt + 0, rt.ghost_off, [&](const RhsMember32& M, long long lu) {
+            const Geom g = member_geom(M);
+            const long long t = lu * BATCH_THREADS + threadIdx.x;
+            if (t < ghost_count(g))
+                ghost_state_cell_packed(g, member_phys(M), (float4*)M.qa, (float4*)M.qb, M.scal, (int)t);
+        });
+        grid_barrier(bar, nb, err);
+        if (blockIdx.x == 0 && threadIdx.x == 0) cnt[0] = 0ULL;
+        // phase 2: dilatation from the packed records
+        sweep_m(cnt + 1, rt.unit_off, [&](const RhsMember32& M, long long lu) {
+            int i, j, k;
+            unit_ijk(M, lu, i, j, k);
+            if (i < M.mx && j < M.my) {
+                CoefT<float> cf{};
+                for (int d = 0; d < 3; d++)
+                    for (int l = 0; l < 5; l++) cf.c1V[d][l] = M.c1V[d][l];
+                cf.xp = M.xp;
+                dil_point_packed<V>(member_geom(M), cf, M.qa, (float*)M.dil, i, j, k);
+            }
+        });
+        grid_barrier(bar, nb, err);
+        if (blockIdx.x == 0 && threadIdx.x == 0) cnt[1] = 0ULL;
+        // phase 3: dilatation ghosts
+        sweep_m(cnt + 2, rt.ghost_off, [&](const RhsMember32& M, long long lu) {
+            const Geom g = member_geom(M);
+            const long long t = lu * BATCH_THREADS + threadIdx.x;
+            if (t < ghost_count(g)) ghost_scalar_cell<float>(g, (float*)M.dil, (int)t);
+        });
+        grid_barrier(bar, nb, err);
+        if (blockIdx.x == 0 && threadIdx.x == 0) cnt[2] = 0ULL;
+        // phase 4: RHS + stage update + the new state's recovery (the standalone point body,
+        // compile-time weights)
+        sweep_m(cnt + 3, rt.unit_off, [&](const RhsMember32& M, long long lu) {
+            int i, j, k;
+            unit_ijk(M, lu, i, j, k);
+            if (i < M.mx && j < M.my) rhs_point_member<S, V>(M, quirk, i, j, k);
+        });
+    } else {
     // phase 1: ghost cells of the stencil inputs of the current state
     sweep(cnt + 0, ctl->ghost_off, ngu, [&](long long u, int q) {
         const BatchInst<R>& I = tab[q];
@@ -297,23 +386,7 @@ __global__ void __launch_bounds__(BATCH_THREADS, sizeof(R) == 4 ? 7 : 4)
     if (blockIdx.x == 0 && threadIdx.x == 0) cnt[2] = 0ULL;
     // phase 4: RHS + stage update into the other state buffer + that state's recovery, every
     // neighbour from global memory (the standalone RHS kernel's point body, compile-time
-    // weights). FP32 batches of up to RHS_TABLE_MAX members read a unit's member parameters
-    // from the kernel argument table; otherwise they are staged in shared memory when the
-    // member changes.
-    if constexpr (sizeof(R) == 4 && TBL) {
-        {
-            sweep(cnt + 3, rt.unit_off, npu, [&](long long u, int q) {
-                const RhsMember32& M = rt.m[q];
-                const long long lu = u - rt.unit_off[q];
-                const long long pl = (long long)M.nbx * M.nby;
-                const int k = (int)(lu / pl);
-                const int rr = (int)(lu - (long long)k * pl);
-                const int by = rr / M.nbx, bx = rr - by * M.nbx;
-                const int i = bx * 32 + tx, j = by * 4 + ty;
-                if (i < M.mx && j < M.my) rhs_point_member<S, V>(M, quirk, i, j, k);
-            });
-        }
-    } else {
+    // weights); the member's parameters are staged in shared memory when it changes
     __shared__ StageParams<R> sp;
     int qs = -1;
     sweep(cnt + 3, ctl->unit_off, npu, [&](long long u, int q) {

@@ -73,18 +73,16 @@ __device__ __forceinline__ R d2x_nu(const Get& get, const R* __restrict__ cvsx, 
     return s;
 }
 
-// Contribution of direction DIR (deviceRHSX/Y/Z). The viscous momentum terms
+// FP64 body: contribution of direction DIR (deviceRHSX/Y/Z) on the separate stencil fields,
+// the velocity gradients from the gradient kernel. The viscous momentum terms
 // (grad mu . s + mu lap u + mu/3 grad theta) of all directions are summed in W[] and the
 // dissipation / conduction in diss / cond, so the energy equation's u_i W_i work term
 // and the mu multiplications are applied once per point instead of once per direction.
+// (The FP32-RHS mode has its own body on the packed records, rhs_dir_packed below.)
 template <typename R, int S, int V, int DIR, class NB>
 __device__ __forceinline__ void rhs_direction(const Geom& g, const CoefT<R>& cf, const NB& nb, int i,
                                               R (&Gr)[9], R th0, R m0, R m3, R u0, R v0, R w0, R r0, R h0,
                                               int quirk, R (&acc)[5], R (&W)[3], R& diss, R& cond, R& dmu_dir) {
-    // FP32: the nine velocity gradients are formed here from the stencils loaded below
-    // (Gr[3 DIR + q] in this direction's pass) and the stress terms, which need gradients
-    // of all directions, are applied after the three passes (rhs_point_nb)
-    constexpr bool GI = sizeof(R) == 4;
     const bool nux = (DIR == 0) && g.nonuniform_x;
     const R xpi = nux ? cf.xp[i] : (R)1;
     const R* c1V = cf.c1V[DIR];
@@ -92,8 +90,8 @@ __device__ __forceinline__ void rhs_direction(const Geom& g, const CoefT<R>& cf,
     const R* c2V = cf.c2V[DIR];
 
     // stress row tau_{DIR, c} / mu  (uXtmp, vXtmp, wXtmp of deviceRHSX and its y/z twins)
-    R tau[3] = {0, 0, 0};
-    if constexpr (!GI) {
+    R tau[3];
+    {
 #pragma unroll
         for (int q = 0; q < 3; q++)
             tau[q] = (q == DIR) ? (R)2 * Gr[3 * DIR + q] - (R)(2. / 3.) * th0 : Gr[3 * DIR + q] + Gr[3 * q + DIR];
@@ -120,14 +118,6 @@ __device__ __forceinline__ void rhs_direction(const Geom& g, const CoefT<R>& cf,
     const auto gp = [&](int l) { return nb.p(l); };
     const R dmu = d1<R, V>(gm, c1V) * xpi;
     dmu_dir = dmu;
-    if constexpr (GI) {   // the gradients of u, v, w along DIR, as the gradient kernel forms them
-        const auto gu = [&](int l) { return us[S + l]; };
-        const auto gv = [&](int l) { return vs[S + l]; };
-        const auto gw = [&](int l) { return ws[S + l]; };
-        R a = d1<R, V>(gu, c1V), b = d1<R, V>(gv, c1V), e2 = d1<R, V>(gw, c1V);
-        if (nux) { a *= xpi; b *= xpi; e2 *= xpi; }
-        Gr[3 * DIR + 0] = a; Gr[3 * DIR + 1] = b; Gr[3 * DIR + 2] = e2;
-    }
     R d2uu, d2vv, d2ww, d2tt;
     if (nux) {
         R a = (R)0, b = (R)0, e2 = (R)0;
@@ -151,15 +141,9 @@ __device__ __forceinline__ void rhs_direction(const Geom& g, const CoefT<R>& cf,
         d2uu = a; d2vv = b; d2ww = e2;
         d2tt = d2u<R, V>(gt, c2V);
     }
-    if constexpr (GI) {
-        W[0] = fma(d2uu, m0, W[0]);
-        W[1] = fma(d2vv, m0, W[1]);
-        W[2] = fma(d2ww, m0, W[2]);
-    } else {
-        W[0] = fma(tau[0], dmu, fma(d2uu, m0, W[0]));
-        W[1] = fma(tau[1], dmu, fma(d2vv, m0, W[1]));
-        W[2] = fma(tau[2], dmu, fma(d2ww, m0, W[2]));
-    }
+    W[0] = fma(tau[0], dmu, fma(d2uu, m0, W[0]));
+    W[1] = fma(tau[1], dmu, fma(d2vv, m0, W[1]));
+    W[2] = fma(tau[2], dmu, fma(d2ww, m0, W[2]));
     // heat conduction lambda d2T + dlambda dT = (lambda/mu) (mu d2T + dmu dT); the ratio
     // is applied once per point
     const R dt = d1<R, V>(gt, c1V) * xpi;
@@ -315,18 +299,16 @@ __device__ __forceinline__ void stage_tail(const Geom& g, const Update<R>& up, d
     if (up.fuse) state_store<R>(up.ph, up.dnext, scal, c, qn[0], inv, un, vn, wn, qn[4]);
 }
 
-// RHS + stage update of one interior point (i, ., k) at element c, with the neighbours
+// FP64 RHS + stage update of one interior point (i, ., k) at element c, with the neighbours
 // along x, y, z from the accessors nx, ny, nz and the centre values given
 template <typename R, int S, int V, class NX, class NY, class NZ>
 __device__ __forceinline__ void rhs_point_nb(const Geom& g, const CoefT<R>& cf, const RhsIn<R>& in,
                                              const Update<R>& up, double* __restrict__ scal, int quirk, int i,
                                              int k, int c, const NX& nx, const NY& ny, const NZ& nz, R th0,
                                              R m0, R u0, R v0, R w0, R r0, R h0) {
-    R Gr[9];
-    if constexpr (sizeof(R) == 8) {   // FP64: the gradient kernel's fields; FP32: formed in the passes
+    R Gr[9];   // the gradient kernel's fields
 #pragma unroll
-        for (int q = 0; q < 9; q++) Gr[q] = ld(in.g[q], c);
-    }
+    for (int q = 0; q < 9; q++) Gr[q] = ld(in.g[q], c);
     const R m3 = m0 * (R)(1.0 / 3.0);
     R acc[5] = {0, 0, 0, 0, 0};
     R W[3] = {0, 0, 0};
@@ -335,24 +317,6 @@ __device__ __forceinline__ void rhs_point_nb(const Geom& g, const CoefT<R>& cf, 
     rhs_direction<R, S, V, 0>(g, cf, nx, i, Gr, th0, m0, m3, u0, v0, w0, r0, h0, quirk, acc, W, diss, cond, dmu[0]);
     rhs_direction<R, S, V, 1>(g, cf, ny, i, Gr, th0, m0, m3, u0, v0, w0, r0, h0, quirk, acc, W, diss, cond, dmu[1]);
     rhs_direction<R, S, V, 2>(g, cf, nz, i, Gr, th0, m0, m3, u0, v0, w0, r0, h0, quirk, acc, W, diss, cond, dmu[2]);
-    if constexpr (sizeof(R) == 4) {
-        // stress rows, dissipation and grad(mu) . s of every direction, now that all nine
-        // gradients are known
-#pragma unroll
-        for (int d = 0; d < 3; d++) {
-            R tau[3];
-#pragma unroll
-            for (int q = 0; q < 3; q++)
-                tau[q] = (q == d) ? (R)2 * Gr[3 * d + q] - (R)(2. / 3.) * th0 : Gr[3 * d + q] + Gr[3 * q + d];
-            const R dw = (d == 1 && quirk) ? Gr[7] : Gr[3 * d + 2];
-            diss = fma(tau[0], Gr[3 * d + 0], diss);
-            diss = fma(tau[1], Gr[3 * d + 1], diss);
-            diss = fma(tau[2], dw, diss);
-            W[0] = fma(tau[0], dmu[d], W[0]);
-            W[1] = fma(tau[1], dmu[d], W[1]);
-            W[2] = fma(tau[2], dmu[d], W[2]);
-        }
-    }
     acc[1] += W[0];
     acc[2] += W[1];
     acc[3] += W[2];

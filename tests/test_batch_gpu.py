@@ -166,3 +166,25 @@ def test_bounded_barrier_gives_up(gpu_lib):
     flag = ctypes.c_int(-1)
     assert gpu_lib.cns_selftest_barrier_timeout(0, 2000, ctypes.byref(flag)) == 0
     assert flag.value == 1
+
+
+def test_persistent_fp32_batch_beyond_the_member_table(gpu_lib):
+    """An FP32 batch of more members than the persistent kernel's argument table holds (64)
+    runs its RHS phase with the members' parameters staged in shared memory: members of
+    uneven size and physics still equal their standalone solvers."""
+    n = 66
+    ms = []
+    for q in range(n):
+        p = tgv_params(10 + (q % 4) * 2, precision=PREC_FP32_RHS, my=9 + q % 3, mz=10 + q % 5,
+                       Re=400.0 + 37.0 * q, Ma=0.1 + 0.005 * q)
+        ms.append((p, smooth_random_state(p, seed=100 + q)))
+    bt = Batch(precision=PREC_FP32_RHS)
+    bt.set_mode(0)
+    ids = [bt.add(p, f, max_steps=8) for p, f in ms]
+    bt.step(3)
+    for q in (0, 1, 31, 64, 65):
+        p, f = ms[q]
+        s = Solver(p)
+        s.copy_field_in(*f)
+        s.run(3)
+        assert max(state_errors(bt.fields(ids[q]), s.copy_field_out())) <= 1e-6, q
