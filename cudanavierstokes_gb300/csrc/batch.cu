@@ -240,6 +240,7 @@ RhsTable<float> rhs_table(const cns_batch* b, int s, int cur) {
             for (int l = 0; l < 5; l++) M.c1V[d][l] = I.cf.c1V[d][l];
         t.unit_off[q + 1] = t.unit_off[q] + (long long)I.nbx * I.nby * I.g.mz;
         t.ghost_off[q + 1] = t.ghost_off[q] + (ghost_count(I.g) + BATCH_THREADS - 1) / BATCH_THREADS;
+        t.col_off[q + 1] = t.col_off[q] + (long long)I.nbx * I.nby * ((I.g.mz + COL_NZ - 1) / COL_NZ);
     }
     return t;
 }

@@ -140,6 +140,7 @@ __device__ __forceinline__ void unit_point(const BatchInst<R>& I, long long lu, 
 // every point (a one-member batch ran at 2,295 against 3,333 Mpoint-steps/s with them in
 // the constant bank); larger batches take that path (n = 0 in the table).
 constexpr int RHS_TABLE_MAX = 64;
+constexpr int COL_NZ = 8;   // planes of a theta column unit (the table path's phase 2)
 
 struct RhsMember32 {
     long long base;
@@ -175,6 +176,7 @@ struct RhsTable<float> {
     int n;                                     // members in the table; 0: use the shared-memory path
     long long unit_off[RHS_TABLE_MAX + 1];     // point-unit prefix offsets (as BatchCtl's)
     long long ghost_off[RHS_TABLE_MAX + 1];    // ghost-unit prefix offsets
+    long long col_off[RHS_TABLE_MAX + 1];      // theta-column prefix offsets (32 x 4 x COL_NZ columns)
     RhsMember32 m[RHS_TABLE_MAX];
 };
 // kernel arguments are limited to 32,764 bytes; the stage kernel's others take < 100
@@ -313,18 +315,24 @@ __global__ void __launch_bounds__(BATCH_THREADS, sizeof(R) == 4 ? 7 : 4)
         });
         grid_barrier(bar, nb, err);
         if (blockIdx.x == 0 && threadIdx.x == 0) cnt[0] = 0ULL;
-        // phase 2: dilatation from the packed records
-        sweep_m(cnt + 1, rt.unit_off, [&](const RhsMember32& M, long long lu) {
-            int i, j, k;
-            unit_ijk(M, lu, i, j, k);
-            if (i < M.mx && j < M.my) {
+        // phase 2: dilatation from the packed records, by columns of 32 x 4 points marching
+        // COL_NZ planes (the standalone z-marching body, halos in shared memory)
+        {
+            __shared__ float su[4][32 + 2 * V], sv[4 + 2 * V][32];
+            sweep_m(cnt + 1, rt.col_off, [&](const RhsMember32& M, long long lu) {
+                const int nbz = (M.mz + COL_NZ - 1) / COL_NZ;
+                const int bz = (int)(lu % nbz);
+                const int r2 = (int)(lu / nbz);
+                const int by = r2 / M.nbx, bx = r2 - by * M.nbx;
                 CoefT<float> cf{};
                 for (int d = 0; d < 3; d++)
                     for (int l = 0; l < 5; l++) cf.c1V[d][l] = M.c1V[d][l];
                 cf.xp = M.xp;
-                dil_point_packed<V>(member_geom(M), cf, M.qa, (float*)M.dil, i, j, k);
-            }
-        });
+                const int k0 = bz * COL_NZ;
+                dil_column_packed<V, 4>(member_geom(M), cf, M.qa, (float*)M.dil, bx * 32, by * 4, k0,
+                                        min(k0 + COL_NZ, M.mz), false, tx, ty, su, sv);
+            });
+        }
         grid_barrier(bar, nb, err);
         if (blockIdx.x == 0 && threadIdx.x == 0) cnt[1] = 0ULL;
         // phase 3: dilatation ghosts

@@ -38,18 +38,8 @@ __global__ void __launch_bounds__(128) k_grad(Geom g, CoefT<R> cf, const R* __re
     grad_point<R, V, sizeof(R) == 4>(g, cf, u, v, w, o, i, j, (int)blockIdx.z, own != 0);
 }
 
-// FP32-RHS dilatation from the packed records (rho, u, v, w), marching in z.
-//
-// A block of 32 x 8 threads owns a 32 x 8 tile of x-y points and walks DIL_NZ (8) consecutive
-// planes. Per plane every thread loads its own record once (u into the x-halo row tile, v
-// into the y-halo column tile in shared memory) and the record V planes ahead, whose w
-// enters a register ring holding w at k - V .. k + V; the threads at the tile edges also
-// load the x and y halos. That is about 3.25 record loads per point instead of the 6V of a
-// point-per-thread stencil (each record is 16 bytes of which one value is used). The loads
-// of plane k + 1 are issued before plane k is computed. The arithmetic per point is
-// grad_point's (DIL_ONLY): the same sums in the same order.
-// Tile slots outside [-V, mx + V) x [-V, my + V) are never read by an interior point and
-// are not loaded; every loaded slot lies in the ghosted allocation (G = S >= V).
+// FP32-RHS dilatation from the packed records (rho, u, v, w), marching in z: blocks of
+// 32 x 8 threads, DIL_NZ (8) planes each (dil_column_packed, kernels_point.cuh).
 constexpr int DIL_TX = 32, DIL_TY = 8, DIL_NZ = 8;
 
 template <int V>
@@ -57,68 +47,9 @@ __global__ void __launch_bounds__(DIL_TX * DIL_TY) k_dil_march(Geom g, CoefT<flo
                                                                float* __restrict__ dil, int own) {
     __shared__ float su[DIL_TY][DIL_TX + 2 * V];   // u of the tile rows, x halo V on each side
     __shared__ float sv[DIL_TY + 2 * V][DIL_TX];   // v of the tile columns, y halo V on each side
-    const int tx = threadIdx.x, ty = threadIdx.y;
-    const int i0 = blockIdx.x * DIL_TX, j0 = blockIdx.y * DIL_TY, k0 = blockIdx.z * DIL_NZ;
-    const int i = i0 + tx, j = j0 + ty;
-    const bool inside = i < g.mx && j < g.my;
-    const bool ghosted = i < g.mx + V && j < g.my + V;   // own slot of the tiles is read by someone
-    const int k1 = min(k0 + DIL_NZ, g.mz);
-    const int P = (int)g.P, PS = (int)g.PS;
-    const int c0 = (int)g.at(i, j, 0);   // element of (i, j, 0); plane k adds k * PS
-    float xp = 1.0f;
-    if (g.nonuniform_x && inside) xp = cf.xp[i];
-    // w at planes k - V .. k + V (ring[V] = the current plane)
-    float ring[2 * V + 1];
-#pragma unroll
-    for (int l = 0; l < 2 * V; l++) ring[l] = inside ? __ldg(qa + c0 + (k0 - V + l) * PS).w : 0.0f;
-    // the loads of plane k: w at k + V, the own record's u and v, the x and y halos;
-    // the next plane's are issued before the current plane is computed (software pipeline)
-    float nw = 0.f, nu = 0.f, nv = 0.f, hxl = 0.f, hxr = 0.f, hyl = 0.f, hyr = 0.f;
-    const auto fetch = [&](int k) {
-        const int ck = c0 + k * PS;
-        nw = inside ? __ldg(qa + ck + V * PS).w : 0.0f;
-        if (ghosted) {
-            const float4 rec = __ldg(qa + ck);
-            nu = rec.y;
-            nv = rec.z;
-        }
-        if (tx < V && j < g.my) hxl = __ldg(qa + ck - V).y;                               // x = i - V >= -V
-        if (tx >= DIL_TX - V && i < g.mx && j < g.my) hxr = __ldg(qa + ck + V).y;          // x = i + V < mx + V
-        if (ty < V && i < g.mx) hyl = __ldg(qa + ck - V * P).z;                           // y = j - V >= -V
-        if (ty >= DIL_TY - V && j < g.my && i < g.mx) hyr = __ldg(qa + ck + V * P).z;      // y = j + V < my + V
-    };
-    fetch(k0);
-    for (int k = k0; k < k1; k++) {
-        const float cw = nw, cu = nu, cv = nv, cxl = hxl, cxr = hxr, cyl = hyl, cyr = hyr;
-        if (k + 1 < k1) fetch(k + 1);
-        ring[2 * V] = cw;
-        const int ck = c0 + k * PS;
-        __syncthreads();   // the previous plane's tiles are no longer read
-        su[ty][tx + V] = cu;
-        sv[ty + V][tx] = cv;
-        if (tx < V) su[ty][tx] = cxl;
-        if (tx >= DIL_TX - V) su[ty][tx + 2 * V] = cxr;
-        if (ty < V) sv[ty][tx] = cyl;
-        if (ty >= DIL_TY - V) sv[ty + 2 * V][tx] = cyr;
-        __syncthreads();
-        if (inside) {
-            float sx = cf.c1V[0][1] * (su[ty][tx + V + 1] - su[ty][tx + V - 1]);
-            float sy = cf.c1V[1][1] * (sv[ty + V + 1][tx] - sv[ty + V - 1][tx]);
-            float sz = cf.c1V[2][1] * (ring[V + 1] - ring[V - 1]);
-#pragma unroll
-            for (int kk = 2; kk <= V; kk++) {
-                sx = fma(cf.c1V[0][kk], su[ty][tx + V + kk] - su[ty][tx + V - kk], sx);
-                sy = fma(cf.c1V[1][kk], sv[ty + V + kk][tx] - sv[ty + V - kk][tx], sy);
-                sz = fma(cf.c1V[2][kk], ring[V + kk] - ring[V - kk], sz);
-            }
-            if (g.nonuniform_x) sx *= xp;
-            const float th = sx + sy + sz;
-            dil[ck] = th;
-            if (own) dil_ghost_owner<float>(g, dil, ck, i, j, k, th);
-        }
-#pragma unroll
-        for (int l = 0; l < 2 * V; l++) ring[l] = ring[l + 1];
-    }
+    const int k0 = blockIdx.z * DIL_NZ;
+    dil_column_packed<V, DIL_TY>(g, cf, qa, dil, blockIdx.x * DIL_TX, blockIdx.y * DIL_TY, k0,
+                                 min(k0 + DIL_NZ, g.mz), own != 0, (int)threadIdx.x, (int)threadIdx.y, su, sv);
 }
 
 template <typename R>

@@ -391,6 +391,83 @@ __device__ __forceinline__ void dil_point_packed(const Geom& g, const CoefT<floa
     if (own) dil_ghost_owner<float>(g, dil, c, i, j, k, th);
 }
 
+// FP32-RHS dilatation of a column of points from the packed records (rho, u, v, w): the
+// threads (tx, ty), tx < 32, ty < TY, own the x-y tile [i0, i0 + 32) x [j0, j0 + TY) and march
+// the planes [k0, k1). Per plane every thread loads its own record once (u into the x-halo
+// row tile su, v into the y-halo column tile sv in shared memory) and the record V planes
+// ahead, whose w enters a register ring holding w at k - V .. k + V; threads at the tile
+// edges also load the x and y halos; the next plane's loads are issued before the current
+// plane is computed. About 2 + 2V/TY + 2V/32 record loads per point instead of the 6V of a
+// point-per-thread stencil (each record is 16 bytes of which one value is used); the
+// arithmetic per point is grad_point's (DIL_ONLY): the same sums in the same order. Tile
+// slots outside [-V, mx + V) x [-V, my + V) are never read by an interior point and are not
+// loaded; every loaded slot lies in the ghosted allocation (G = S >= V). All threads of the
+// block call it (it synchronises the block).
+template <int V, int TY>
+__device__ __forceinline__ void dil_column_packed(const Geom& g, const CoefT<float>& cf, const float4* __restrict__ qa,
+                                                  float* __restrict__ dil, int i0, int j0, int k0, int k1, bool own,
+                                                  int tx, int ty, float (*su)[32 + 2 * V], float (*sv)[32]) {
+    static_assert(V <= TY, "the y halo rows are loaded by the first and last V tile rows");
+    const int i = i0 + tx, j = j0 + ty;
+    const bool inside = i < g.mx && j < g.my;
+    const bool ghosted = i < g.mx + V && j < g.my + V;   // own slot of the tiles is read by someone
+    const int P = (int)g.P, PS = (int)g.PS;
+    const int c0 = (int)g.at(i, j, 0);   // element of (i, j, 0); plane k adds k * PS
+    float xp = 1.0f;
+    if (g.nonuniform_x && inside) xp = cf.xp[i];
+    // w at planes k - V .. k + V (ring[V] = the current plane)
+    float ring[2 * V + 1];
+#pragma unroll
+    for (int l = 0; l < 2 * V; l++) ring[l] = inside ? __ldg(qa + c0 + (k0 - V + l) * PS).w : 0.0f;
+    // the loads of plane k: w at k + V, the own record's u and v, the x and y halos
+    float nw = 0.f, nu = 0.f, nv = 0.f, hxl = 0.f, hxr = 0.f, hyl = 0.f, hyr = 0.f;
+    const auto fetch = [&](int k) {
+        const int ck = c0 + k * PS;
+        nw = inside ? __ldg(qa + ck + V * PS).w : 0.0f;
+        if (ghosted) {
+            const float4 rec = __ldg(qa + ck);
+            nu = rec.y;
+            nv = rec.z;
+        }
+        if (tx < V && j < g.my) hxl = __ldg(qa + ck - V).y;                           // x = i - V >= -V
+        if (tx >= 32 - V && i < g.mx && j < g.my) hxr = __ldg(qa + ck + V).y;          // x = i + V < mx + V
+        if (ty < V && i < g.mx) hyl = __ldg(qa + ck - V * P).z;                       // y = j - V >= -V
+        if (ty >= TY - V && j < g.my && i < g.mx) hyr = __ldg(qa + ck + V * P).z;      // y = j + V < my + V
+    };
+    if (k0 < k1) fetch(k0);
+    for (int k = k0; k < k1; k++) {
+        const float cw = nw, cu = nu, cv = nv, cxl = hxl, cxr = hxr, cyl = hyl, cyr = hyr;
+        if (k + 1 < k1) fetch(k + 1);
+        ring[2 * V] = cw;
+        const int ck = c0 + k * PS;
+        __syncthreads();   // the previous plane's tiles are no longer read
+        su[ty][tx + V] = cu;
+        sv[ty + V][tx] = cv;
+        if (tx < V) su[ty][tx] = cxl;
+        if (tx >= 32 - V) su[ty][tx + 2 * V] = cxr;
+        if (ty < V) sv[ty][tx] = cyl;
+        if (ty >= TY - V) sv[ty + 2 * V][tx] = cyr;
+        __syncthreads();
+        if (inside) {
+            float sx = cf.c1V[0][1] * (su[ty][tx + V + 1] - su[ty][tx + V - 1]);
+            float sy = cf.c1V[1][1] * (sv[ty + V + 1][tx] - sv[ty + V - 1][tx]);
+            float sz = cf.c1V[2][1] * (ring[V + 1] - ring[V - 1]);
+#pragma unroll
+            for (int kk = 2; kk <= V; kk++) {
+                sx = fma(cf.c1V[0][kk], su[ty][tx + V + kk] - su[ty][tx + V - kk], sx);
+                sy = fma(cf.c1V[1][kk], sv[ty + V + kk][tx] - sv[ty + V - kk][tx], sy);
+                sz = fma(cf.c1V[2][kk], ring[V + kk] - ring[V - kk], sz);
+            }
+            if (g.nonuniform_x) sx *= xp;
+            const float th = sx + sy + sz;
+            dil[ck] = th;
+            if (own) dil_ghost_owner<float>(g, dil, ck, i, j, k, th);
+        }
+#pragma unroll
+        for (int l = 0; l < 2 * V; l++) ring[l] = ring[l + 1];
+    }
+}
+
 // Dilatation ghost cell t (BCxNumber2 / BCyNumber1 / BCzNumber1): x periodic | wall:
 // even | boundary layer: bottom even, top extrapolated; y periodic; z periodic | extrapolated.
 template <typename R>
