@@ -257,11 +257,11 @@ def run_batched(args, stream_ptr, members=48, mode_req="tuned", with_other=True)
     out["other_mode"] = {"mode": names[other], "value": pts * args.steps / (oms * 1e-3) / 1e6,
                          "ms_per_step": oms / args.steps}
     if mode == 1:
-        out["why_mode"] = ("the persistent kernel runs the same point bodies, but a member's parameters reach "
-                           "them from a kernel-argument table indexed by member (registers and ~30 spill loads "
-                           "per point in the RHS phase) instead of as constant-bank operands, with compile-time "
-                           "stencil weights scaled by the spacings (+7 %) and point-per-thread theta; the "
-                           "concurrent mode keeps the standalone kernels (profiles/batch_stage_persistent_fp32.md)")
+        out["why_mode"] = ("the persistent kernel runs the standalone point bodies over all members with the "
+                           "members' parameters from a kernel-argument table (uniform per member loop), but "
+                           "with compile-time stencil weights scaled by each member's spacings (+7 % on the RHS) "
+                           "and a grid barrier after each phase; the concurrent mode's standalone kernels keep "
+                           "premultiplied weights as constant-bank operands (profiles/batch_stage_persistent_fp32.md)")
     if other == 0:
         out["other_mode"]["launch_shape"] = {"threads": 128, "blocks_per_sm": bt.shape()[1]}
     bt.close()
