@@ -462,9 +462,9 @@ def fp32_roofline(N, S, V, ph, fp32_peak):
            "fp32": {"achieved": tf, "peak": fp32_peak, "unit": "TFLOP/s", "frac": tf / fp32_peak,
                     "peak_source": "measured live (FMA-chain probe, cns_probe_fma_peak)"},
            "phase_ms": ph}
-    if "fp64_inst_per_point" in kv:
-        out["executed"] = {k: float(v) for k, v in kv.items() if k.endswith(("_per_point", "_pct"))}
-        out["executed"]["source"] = "ncu --set full, profiles/rhs_kernel_channel_fp32.md"
+    executed = {k: float(v) for k, v in kv.items() if k.endswith(("_per_point", "_pct"))}
+    if executed:
+        out["executed"] = dict(executed, source="ncu --set full, profiles/rhs_kernel_channel_fp32.md")
     return out
 
 

@@ -35,3 +35,28 @@ def test_traffic_scales_with_points():
         assert bench.read_traffic(2 * int(kv["points"]), fp32=fp32) == pytest.approx(
             2 * float(kv["dram_bytes_per_launch"]))
     assert bench.read_traffic(1000, fp32=True) < bench.read_traffic(1000)
+
+
+def test_fp32_roofline_object():
+    """The FP32-RHS leg's roofline: algorithmic bytes against the measured HBM bandwidth, the
+    FP32 flop rate against the given FMA peak, the ncu traffic and the executed counters of
+    the committed summary."""
+    from cudanavierstokes_gb300 import roofline as rf
+    N = 3932160
+    ph = {"ghost_ms": 0.0135, "grad_ms": 0.0361, "rhs_ms": 0.25}
+    r = bench.fp32_roofline(N, 4, 4, ph, 70.0)
+    assert r["bound"] == "hbm" and r["unit"] == "GB/s"
+    assert r["achieved"] == pytest.approx(rf.RHS_KERNEL_BYTES * N / 0.25e-3 / 1e9)
+    assert r["frac"] == pytest.approx(r["achieved"] / r["peak"])
+    assert r["fp32"]["frac"] == pytest.approx(r["fp32"]["achieved"] / 70.0)
+    assert r["traffic"] == pytest.approx(bench.read_traffic(N, fp32=True))
+    assert r["executed"]["global_ld_per_point"] > 0 and 0 < r["executed"]["fp64_pipe_active_pct"] <= 100
+
+
+def test_reference_arm_times_the_full_grid(monkeypatch):
+    """--impl reference measures the configured channel grid itself (no extrapolation from a
+    sample): the oracle is set up on the workload's own parameters."""
+    monkeypatch.setattr(sys, "argv", ["bench.py", "--impl", "reference"])
+    a = bench.parse_args()
+    p, _ = bench.workload(a.workload, "fp64", a.grid)
+    assert (p.mx, p.my, p.mz) == (128, 160, 192)
