@@ -60,3 +60,18 @@ def test_reference_arm_times_the_full_grid(monkeypatch):
     a = bench.parse_args()
     p, _ = bench.workload(a.workload, "fp64", a.grid)
     assert (p.mx, p.my, p.mz) == (128, 160, 192)
+
+
+def test_reference_arm_line(monkeypatch, capsys, oracle_mod):
+    """The reference arm end to end on a small channel: one JSON line with the arm's tag, the
+    metric and its own cpu_baseline and e2e (no host-device copies)."""
+    import json
+    monkeypatch.setattr(sys, "argv", ["bench.py", "--impl", "reference", "--grid", "16,12,20", "--steps", "2",
+                                      "--warmup", "1"])
+    bench.main()
+    line = json.loads(capsys.readouterr().out.strip().splitlines()[-1])
+    assert line["impl"] == "reference" and line["metric"] == bench.METRIC and line["steps"] == 2
+    assert line["value"] > 0 and line["cpu_baseline"]["value"] == line["value"]
+    assert line["cpu_baseline"]["kind"] == "port" and line["cpu_baseline"]["cores"] >= 1
+    assert line["e2e"]["h2d_bytes_per_step"] == 0 and line["e2e"]["value"] == line["value"]
+    assert line["config"]["grid"] == [16, 12, 20]
