@@ -33,10 +33,10 @@ using namespace cns;
 namespace cns {
 void launch_batch_stage_fp64(int S, int V, dim3 grid, const BatchInst<double>* tab, const BatchCtl* ctl, int cur,
                              int stage, int quirk, unsigned* bar, int* err, unsigned long long* cnt,
-                             const RhsTable<double>& rt, cudaStream_t s);
+                             const MemberTable<double>& rt, cudaStream_t s);
 void launch_batch_stage_fp32(int S, int V, dim3 grid, const BatchInst<float>* tab, const BatchCtl* ctl, int cur,
                              int stage, int quirk, unsigned* bar, int* err, unsigned long long* cnt,
-                             const RhsTable<float>& rt, cudaStream_t s);
+                             const MemberTable<float>& rt, cudaStream_t s);
 void launch_batch_time_fp64(const BatchInst<double>* tab, const BatchCtl* ctl, cudaStream_t s);
 void launch_batch_time_fp32(const BatchInst<float>* tab, const BatchCtl* ctl, cudaStream_t s);
 int batch_stage_occupancy(int fp32, int S, int V, int* blocks_per_sm);
@@ -88,7 +88,7 @@ struct cns_batch {
     BatchCtl* d_ctl = nullptr;
     unsigned* d_bar = nullptr;
     unsigned long long* d_cnt = nullptr;   // the persistent kernel's four phase unit counters
-    std::vector<BatchInst<float>> h_tab32;   // host copy of the FP32 member table (RHS-phase argument)
+    std::vector<BatchInst<float>> h_tab32;   // host copy of the FP32 member table (the launch argument's source)
     int* d_err = nullptr;
     int threads = 128, blocks_per_sm = 1, nsm = 152;
     bool tuned = false;
@@ -190,7 +190,7 @@ int upload_table(cns_batch* b) {
     BCK(cudaMemcpyAsync(b->d_ctl, &ctl, sizeof ctl, cudaMemcpyHostToDevice, b->stream));
     BCK(cudaStreamSynchronize(b->stream));
     if constexpr (sizeof(R) == 4) {
-        // the RHS phase's member table is a launch argument, baked into the captured steps
+        // the member table is a launch argument, baked into the captured steps
         b->h_tab32.assign(tab.begin(), tab.begin() + n);
         b->drop_graphs();
     }
@@ -202,19 +202,19 @@ int upload(cns_batch* b) {
     return b->precision == CNS_PREC_FP32_RHS ? upload_table<float>(b) : upload_table<double>(b);
 }
 
-// The RHS phase's member table for stage s from parity cur: FP32 batches of up to
-// RHS_TABLE_MAX members (n = 0 otherwise: the kernel stages the parameters in shared memory)
-RhsTable<float> rhs_table(const cns_batch* b, int s, int cur) {
-    RhsTable<float> t;
+// The persistent kernel's member table for stage s from parity cur: FP32 batches of up to
+// MEMBER_TABLE_MAX members (n = 0 otherwise: the kernel reads the device table instead)
+MemberTable<float> member_table(const cns_batch* b, int s, int cur) {
+    MemberTable<float> t;
     std::memset(&t, 0, sizeof t);
     const int n = (int)b->h_tab32.size();
-    if (n > RHS_TABLE_MAX) return t;
+    if (n > MEMBER_TABLE_MAX) return t;
     t.n = n;
     for (int q = 0; q < n; q++) {
         const BatchInst<float>& I = b->h_tab32[q];
         const RhsIn<float>& in = I.in[cur];
         const Update<float>& up = I.up[s][cur];
-        RhsMember32& M = t.m[q];
+        Member32& M = t.m[q];
         M.base = I.g.base; M.P = (int)I.g.P; M.PS = (int)I.g.PS; M.mx = I.g.mx; M.my = I.g.my;
         M.nbx = I.nbx; M.nby = I.nby; M.nonuniform_x = I.g.nonuniform_x;
         M.use_prev = up.use_prev; M.fuse = up.fuse; M.vexp_is_one = up.ph.vexp_is_one;
@@ -255,10 +255,10 @@ int launch_stage(cns_batch* b, int s, int cur) {
     }
     if (f32)
         launch_batch_stage_fp32(b->S, b->V, grid, (const BatchInst<float>*)b->d_tab, b->d_ctl, cur, s, b->quirk,
-                                b->d_bar, b->d_err, b->d_cnt, rhs_table(b, s, cur), b->stream);
+                                b->d_bar, b->d_err, b->d_cnt, member_table(b, s, cur), b->stream);
     else
         launch_batch_stage_fp64(b->S, b->V, grid, (const BatchInst<double>*)b->d_tab, b->d_ctl, cur, s, b->quirk,
-                                b->d_bar, b->d_err, b->d_cnt, RhsTable<double>{0}, b->stream);
+                                b->d_bar, b->d_err, b->d_cnt, MemberTable<double>{0}, b->stream);
     b->launches++;
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) {

@@ -7,7 +7,7 @@ cudaError_t batch_occ_fp64(int S, int V, int* nb);
 
 namespace cns {
 void launch_batch_stage_fp32(int S, int V, dim3 grid, const BatchInst<float>* tab, const BatchCtl* ctl, int cur,
-                             int stage, int quirk, unsigned* bar, int* err, unsigned long long* cnt, const RhsTable<float>& rt,
+                             int stage, int quirk, unsigned* bar, int* err, unsigned long long* cnt, const MemberTable<float>& rt,
                              cudaStream_t s) {
     batch_launch_dispatch<float>(S, V, grid, tab, ctl, cur, stage, quirk, bar, err, cnt, rt, s);
 }

@@ -3,7 +3,7 @@
 
 namespace cns {
 void launch_batch_stage_fp64(int S, int V, dim3 grid, const BatchInst<double>* tab, const BatchCtl* ctl, int cur,
-                             int stage, int quirk, unsigned* bar, int* err, unsigned long long* cnt, const RhsTable<double>& rt,
+                             int stage, int quirk, unsigned* bar, int* err, unsigned long long* cnt, const MemberTable<double>& rt,
                              cudaStream_t s) {
     batch_launch_dispatch<double>(S, V, grid, tab, ctl, cur, stage, quirk, bar, err, cnt, rt, s);
 }

@@ -135,14 +135,14 @@ __device__ __forceinline__ void unit_point(const BatchInst<R>& I, long long lu, 
 
 // FP32-RHS members' parameters as a kernel argument (constant bank): what the four phases'
 // point bodies read of the member's geometry, inverse spacings, boundary constants, packed
-// stencil inputs, Wray stage update and state recovery, for up to RHS_TABLE_MAX members. Read
+// stencil inputs, Wray stage update and state recovery, for up to MEMBER_TABLE_MAX members. Read
 // through shared memory instead, these parameters took registers and issue slots in
 // every point (a one-member batch ran at 2,295 against 3,333 Mpoint-steps/s with them in
 // the constant bank); larger batches take that path (n = 0 in the table).
-constexpr int RHS_TABLE_MAX = 64;
+constexpr int MEMBER_TABLE_MAX = 64;
 constexpr int COL_NZ = 8;   // planes of a theta column unit (the table path's phase 2)
 
-struct RhsMember32 {
+struct Member32 {
     long long base;
     int P, PS, mx, my, nbx, nby, nonuniform_x, use_prev, fuse, vexp_is_one;
     float inv[3], inv2[3], lam_mu, ca, cb, f_vexp, f_invRe;
@@ -168,28 +168,28 @@ struct RhsMember32 {
 };
 
 template <typename R>
-struct RhsTable {     // FP64 members keep the shared-memory path
+struct MemberTable {     // FP64 batches keep the device-table / shared-memory path
     int n;
 };
 template <>
-struct RhsTable<float> {
+struct MemberTable<float> {
     int n;                                     // members in the table; 0: use the shared-memory path
-    long long unit_off[RHS_TABLE_MAX + 1];     // point-unit prefix offsets (as BatchCtl's)
-    long long ghost_off[RHS_TABLE_MAX + 1];    // ghost-unit prefix offsets
-    long long col_off[RHS_TABLE_MAX + 1];      // theta-column prefix offsets (32 x 4 x COL_NZ columns)
-    RhsMember32 m[RHS_TABLE_MAX];
+    long long unit_off[MEMBER_TABLE_MAX + 1];     // point-unit prefix offsets (as BatchCtl's)
+    long long ghost_off[MEMBER_TABLE_MAX + 1];    // ghost-unit prefix offsets
+    long long col_off[MEMBER_TABLE_MAX + 1];      // theta-column prefix offsets (32 x 4 x COL_NZ columns)
+    Member32 m[MEMBER_TABLE_MAX];
 };
 // kernel arguments are limited to 32,764 bytes; the stage kernel's others take < 100
-static_assert(sizeof(RhsTable<float>) <= 32600, "the member table must fit the kernel-argument space");
+static_assert(sizeof(MemberTable<float>) <= 32600, "the member table must fit the kernel-argument space");
 
 // a member's geometry and boundary constants for the ghost and theta phases
-__device__ __forceinline__ Geom member_geom(const RhsMember32& M) {
+__device__ __forceinline__ Geom member_geom(const Member32& M) {
     Geom g{};
     g.mx = M.mx; g.my = M.my; g.mz = M.mz; g.G = M.G; g.P = M.P; g.PS = M.PS; g.base = M.base;
     g.xbc = M.xbc; g.zbl = M.zbl; g.nonuniform_x = M.nonuniform_x; g.dy = M.dy;
     return g;
 }
-__device__ __forceinline__ Phys member_phys(const RhsMember32& M) {
+__device__ __forceinline__ Phys member_phys(const Member32& M) {
     Phys ph{};
     ph.Rgas = M.Rgas; ph.invRe = M.invRe; ph.hcoef = M.hcoef; ph.vexp = M.vexp; ph.vexp_is_one = M.vexp_is_one;
     ph.twall_top = M.twall_top; ph.twall_bot = M.twall_bot; ph.perturbed = M.perturbed;
@@ -201,7 +201,7 @@ __device__ __forceinline__ Phys member_phys(const RhsMember32& M) {
 // the RHS phase's point of member M: the standalone body (compile-time weights) on
 // geometry, coefficients, inputs and stage update assembled from the table entry
 template <int S, int V>
-__device__ __forceinline__ void rhs_point_member(const RhsMember32& M, int quirk, int i, int j, int k) {
+__device__ __forceinline__ void rhs_point_member(const Member32& M, int quirk, int i, int j, int k) {
     Geom g{};
     g.mx = M.mx; g.my = M.my; g.P = M.P; g.PS = M.PS; g.base = M.base; g.nonuniform_x = M.nonuniform_x;
     CoefT<float> cf{};
@@ -244,19 +244,20 @@ struct UnitQueue {
 
 // FP32: 7 blocks of 128 per SM (72 registers); the RHS phase uses the packed body with
 // compile-time stencil weights, so a member's coefficients are six inverse spacings
-// instead of tables. FP64: 4 blocks.
+// instead of tables; theta is computed by columns marching in z. FP64: 4 blocks.
 //
 // cnt[0..3]: the four phases' unit counters, zero at launch; each is reset by block 0 once
 // no block can take from it any more (after the barrier that ends its phase; the RHS
 // phase's counter at the start of the next launch, before its first barrier).
-// TBL: the RHS phase reads the members from the kernel-argument table (FP32, up to
-// RHS_TABLE_MAX members); otherwise through shared memory. Two instantiations, so that
-// neither path's registers constrain the other.
+// TBL: every phase walks the members in an outer loop and reads their parameters from the
+// kernel-argument table (FP32, up to MEMBER_TABLE_MAX members); otherwise the phases look
+// members up per unit in the device table and the RHS phase stages them in shared memory.
+// Two instantiations, so that neither path's registers constrain the other.
 template <typename R, int S, int V, bool TBL>
 __global__ void __launch_bounds__(BATCH_THREADS, sizeof(R) == 4 ? 7 : 4)
     k_batch_stage(const BatchInst<R>* __restrict__ tab, const BatchCtl* __restrict__ ctl, int cur, int stage,
                   int quirk, unsigned* bar, int* err, unsigned long long* cnt,
-                  const __grid_constant__ RhsTable<R> rt) {
+                  const __grid_constant__ MemberTable<R> rt) {
     const int n = ctl->n;
     if (n <= 0) return;
     const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
@@ -286,7 +287,7 @@ __global__ void __launch_bounds__(BATCH_THREADS, sizeof(R) == 4 ? 7 : 4)
         const auto sweep_m = [&](unsigned long long* c, const long long* off, auto&& body) {
             UnitQueue w(c, s_next);
             for (int q = 0; q < rt.n; q++) {
-                const RhsMember32& M = rt.m[q];
+                const Member32& M = rt.m[q];
                 while (w.u < off[q + 1]) {
                     long long mine = 0;
                     if (threadIdx.x == 0) mine = (long long)atomicAdd(c, 1ULL);   // the next unit, in flight
@@ -298,7 +299,7 @@ __global__ void __launch_bounds__(BATCH_THREADS, sizeof(R) == 4 ? 7 : 4)
                 }
             }
         };
-        const auto unit_ijk = [&](const RhsMember32& M, long long lu, int& i, int& j, int& k) {
+        const auto unit_ijk = [&](const Member32& M, long long lu, int& i, int& j, int& k) {
             const long long pl = (long long)M.nbx * M.nby;
             k = (int)(lu / pl);
             const int rr = (int)(lu - (long long)k * pl);
@@ -307,7 +308,7 @@ __global__ void __launch_bounds__(BATCH_THREADS, sizeof(R) == 4 ? 7 : 4)
             j = by * 4 + ty;
         };
         // phase 1: ghost cells of the stencil inputs of the current state
-        sweep_m(cnt + 0, rt.ghost_off, [&](const RhsMember32& M, long long lu) {
+        sweep_m(cnt + 0, rt.ghost_off, [&](const Member32& M, long long lu) {
             const Geom g = member_geom(M);
             const long long t = lu * BATCH_THREADS + threadIdx.x;
             if (t < ghost_count(g))
@@ -319,7 +320,7 @@ __global__ void __launch_bounds__(BATCH_THREADS, sizeof(R) == 4 ? 7 : 4)
         // COL_NZ planes (the standalone z-marching body, halos in shared memory)
         {
             __shared__ float su[4][32 + 2 * V], sv[4 + 2 * V][32];
-            sweep_m(cnt + 1, rt.col_off, [&](const RhsMember32& M, long long lu) {
+            sweep_m(cnt + 1, rt.col_off, [&](const Member32& M, long long lu) {
                 const int nbz = (M.mz + COL_NZ - 1) / COL_NZ;
                 const int bz = (int)(lu % nbz);
                 const int r2 = (int)(lu / nbz);
@@ -336,7 +337,7 @@ __global__ void __launch_bounds__(BATCH_THREADS, sizeof(R) == 4 ? 7 : 4)
         grid_barrier(bar, nb, err);
         if (blockIdx.x == 0 && threadIdx.x == 0) cnt[1] = 0ULL;
         // phase 3: dilatation ghosts
-        sweep_m(cnt + 2, rt.ghost_off, [&](const RhsMember32& M, long long lu) {
+        sweep_m(cnt + 2, rt.ghost_off, [&](const Member32& M, long long lu) {
             const Geom g = member_geom(M);
             const long long t = lu * BATCH_THREADS + threadIdx.x;
             if (t < ghost_count(g)) ghost_scalar_cell<float>(g, (float*)M.dil, (int)t);
@@ -345,7 +346,7 @@ __global__ void __launch_bounds__(BATCH_THREADS, sizeof(R) == 4 ? 7 : 4)
         if (blockIdx.x == 0 && threadIdx.x == 0) cnt[2] = 0ULL;
         // phase 4: RHS + stage update + the new state's recovery (the standalone point body,
         // compile-time weights)
-        sweep_m(cnt + 3, rt.unit_off, [&](const RhsMember32& M, long long lu) {
+        sweep_m(cnt + 3, rt.unit_off, [&](const Member32& M, long long lu) {
             int i, j, k;
             unit_ijk(M, lu, i, j, k);
             if (i < M.mx && j < M.my) rhs_point_member<S, V>(M, quirk, i, j, k);

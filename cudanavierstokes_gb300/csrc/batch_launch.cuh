@@ -6,7 +6,7 @@ namespace cns {
 
 template <typename R, int S, int V>
 cudaError_t batch_launch_t(dim3 grid, const BatchInst<R>* tab, const BatchCtl* ctl, int cur, int stage, int quirk,
-                           unsigned* bar, int* err, unsigned long long* cnt, const RhsTable<R>& rt, cudaStream_t s) {
+                           unsigned* bar, int* err, unsigned long long* cnt, const MemberTable<R>& rt, cudaStream_t s) {
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = grid;
     cfg.blockDim = dim3(BATCH_THREADS);
@@ -24,7 +24,7 @@ cudaError_t batch_launch_t(dim3 grid, const BatchInst<R>* tab, const BatchCtl* c
 
 template <typename R>
 cudaError_t batch_launch_dispatch(int S, int V, dim3 grid, const BatchInst<R>* tab, const BatchCtl* ctl, int cur,
-                                  int stage, int quirk, unsigned* bar, int* err, unsigned long long* cnt, const RhsTable<R>& rt, cudaStream_t s) {
+                                  int stage, int quirk, unsigned* bar, int* err, unsigned long long* cnt, const MemberTable<R>& rt, cudaStream_t s) {
 #define CNS_BL(SS, VV) \
     if (S == SS && V == VV) return batch_launch_t<R, SS, VV>(grid, tab, ctl, cur, stage, quirk, bar, err, cnt, rt, s);
     CNS_BL(1, 1) CNS_BL(2, 1) CNS_BL(2, 2) CNS_BL(3, 1) CNS_BL(3, 2) CNS_BL(3, 3)
