@@ -11,6 +11,8 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include "pow_tables.h"
+
 namespace cns {
 
 enum XBC { XBC_PER = 0, XBC_WALL = 1, XBC_BL = 2 };
@@ -160,56 +162,51 @@ __device__ __forceinline__ double rcp_nr(double x) {
     return fma(r, fma(e, e, e), r);
 }
 
-// x^a in FP64 for the viscosity law mu ~ T^a, as exp(a ln x) with
-//   ln x = k ln2 + 2 atanh(s),  x = 2^k m,  m in [sqrt(2)/2, sqrt(2)),  s = (m-1)/(m+1),
-//     atanh s = s + s^3/3 + ... + s^23/23  (|s| <= 0.172: truncation below 2^-64),
-//   exp y = 2^j exp(r),  j = nearest(y / ln2),  r = y - j ln2 with ln2 split in a 32-bit
-//     head (j ln2_hi exact) and a tail (Cody & Waite's additive range reduction),
-//     exp r = sum r^n / n!, n <= 13  (|r| <= 0.347: truncation below 2^-57).
-// About 40 FP64 operations against ~120 for the library pow, which runs on the FP64
-// pipe. The error of exp(y) is that of y, about |y| ulp, so the series serve
-// |a ln x| < 1 (T^0.7 for 0.24 < T < 4.2, the temperatures of these flows), within a
+// x^a in FP64 for the viscosity law mu ~ T^a, as exp(a ln x) with 64-entry tables
+// (pow_tables.h, generated with 60-digit arithmetic by gen_pow_tables.py):
+//   ln x = k ln2 - ln r_i + ln(1 + d),  x = 2^k m,  m in [1, 2),  i = the top 6 fraction
+//     bits of m,  r_i ~ 1/c_i for the subinterval centre c_i = 1 + (i + 1/2)/64,
+//     d = m r_i - 1 (one rounding, |d| < 2^-7),  ln(1 + d) by its series to d^8
+//     (truncation below 2^-66), ln2 and -ln r_i as double-doubles;
+//   exp y = 2^(j/64) exp(r),  j = nearest(64 y / ln2),  r = y - j ln2/64 with ln2/64 split
+//     in a 41-bit head (j ln2_hi exact) and a tail (Cody & Waite's reduction), |r| <= 0.0055,
+//     exp(r) - 1 = r + r^2 (1/2 + r/6 + ... + r^4/720) (truncation below 2^-65), 2^(i/64)
+//     as a double-double.
+// About 28 FP64 operations and five table loads (L1-resident) against ~120 for the library
+// pow, which runs on the FP64 pipe. The error of exp(y) is that of y, about |y| ulp, so it
+// serves |a ln x| < 1 (T^0.7 for 0.24 < T < 4.2, the temperatures of these flows), within a
 // few ulp of pow (a GPU test bounds it); other arguments take pow itself.
 __device__ __forceinline__ double pow_visc(double x, double a) {
-    const double LN2_HI = 0.6931471803691238, LN2_LO = 1.9082149292705877e-10;
-    const double INV_LN2 = 1.4426950408889634, SHIFT = 6755399441055744.0;   // 1.5 * 2^52
+    const double INV_LN2_64 = 92.33248261689366, SHIFT = 6755399441055744.0;   // 64/ln2, 1.5 * 2^52
     if (!(x > 1e-300 && x < 1e300)) return pow(x, a);
     const unsigned hx = (unsigned)__double2hiint(x);
-    int k = (int)(hx >> 20) - 1023;
-    unsigned hm = (hx & 0x000fffffu) | 0x3ff00000u;        // m in [1, 2)
-    if (hm >= 0x3ff6a09fu) { hm -= 0x00100000u; k += 1; }  // m in [0.707, 1.414]
-    const double m = __hiloint2double((int)hm, __double2loint(x));
-    const double num = m - 1.0, den = m + 1.0;               // m - 1 exact
-    double inv = f2d(__frcp_rn(d2f(den)));
-    inv = fma(inv, fma(-den, inv, 1.0), inv);
-    inv = fma(inv, fma(-den, inv, 1.0), inv);
-    const double s = num * inv, z = s * s;
-    double p = 1.0 / 23.0;
-    p = fma(p, z, 1.0 / 21.0); p = fma(p, z, 1.0 / 19.0);
-    p = fma(p, z, 1.0 / 17.0); p = fma(p, z, 1.0 / 15.0); p = fma(p, z, 1.0 / 13.0);
-    p = fma(p, z, 1.0 / 11.0); p = fma(p, z, 1.0 / 9.0);  p = fma(p, z, 1.0 / 7.0);
-    p = fma(p, z, 1.0 / 5.0);  p = fma(p, z, 1.0 / 3.0);
-    const double lnm = fma(2.0 * s * z, p, 2.0 * s);         // 2 atanh(s)
+    const int k = (int)(hx >> 20) - 1023;
+    const int i = (int)((hx >> 14) & 63u);                 // top 6 bits of the fraction
+    const double m = __hiloint2double((int)((hx & 0x000fffffu) | 0x3ff00000u), __double2loint(x));
+    const double d = fma(m, __ldg(&kPowRcp[i]), -1.0);
+    double q = -1.0 / 8.0;                                 // ln(1 + d) = d + d^2 q(d)
+    q = fma(q, d, 1.0 / 7.0); q = fma(q, d, -1.0 / 6.0); q = fma(q, d, 1.0 / 5.0);
+    q = fma(q, d, -1.0 / 4.0); q = fma(q, d, 1.0 / 3.0); q = fma(q, d, -0.5);
+    const double l1p = fma(d * d, q, d);
     // k as a double through the 2^52 + 2^31 bias (no conversion instruction)
     const double kd = __hiloint2double(0x43300000, (int)((unsigned)k + 0x80000000u)) -
                       __hiloint2double(0x43300000, (int)0x80000000u);
-    const double lnx = fma(kd, LN2_HI, fma(kd, LN2_LO, lnm));
-    const double y = a * lnx;
+    const double hi = fma(kd, POW_LN2_HI, __ldg(&kPowLnHi[i]));
+    const double lo = fma(kd, POW_LN2_LO, __ldg(&kPowLnLo[i]));
+    const double y = a * (hi + (lo + l1p));
     if (!(fabs(y) < 1.0)) return pow(x, a);
-    const double t = fma(y, INV_LN2, SHIFT);
+    const double t = fma(y, INV_LN2_64, SHIFT);
     const int j = __double2loint(t);
     const double jd = t - SHIFT;
-    double r = fma(-jd, LN2_HI, y);
-    r = fma(-jd, LN2_LO, r);
-    double e = 1.0 / 6227020800.0;                                      // 1/13!
-    e = fma(e, r, 1.0 / 479001600.0); e = fma(e, r, 1.0 / 39916800.0);  // 1/12!, 1/11!
-    e = fma(e, r, 1.0 / 3628800.0);   e = fma(e, r, 1.0 / 362880.0);
-    e = fma(e, r, 1.0 / 40320.0);     e = fma(e, r, 1.0 / 5040.0);
-    e = fma(e, r, 1.0 / 720.0);       e = fma(e, r, 1.0 / 120.0);
-    e = fma(e, r, 1.0 / 24.0);        e = fma(e, r, 1.0 / 6.0);
-    e = fma(e, r, 0.5);               e = fma(e, r, 1.0);
-    e = fma(e, r, 1.0);
-    return __hiloint2double(__double2hiint(e) + (int)((unsigned)j << 20), __double2loint(e));
+    double r = fma(-jd, POW_LN2_64_HI, y);
+    r = fma(-jd, POW_LN2_64_LO, r);
+    double p = 1.0 / 720.0;                                // exp(r) - 1 = r + r^2 p(r)
+    p = fma(p, r, 1.0 / 120.0); p = fma(p, r, 1.0 / 24.0); p = fma(p, r, 1.0 / 6.0); p = fma(p, r, 0.5);
+    const double em1 = fma(r * r, p, r);
+    const int ti = j & 63, e = j >> 6;                     // j = 64 e + ti, e = floor(j / 64)
+    const double th = __ldg(&kPowExpHi[ti]);
+    const double res = th + fma(th, em1, __ldg(&kPowExpLo[ti]));
+    return __hiloint2double(__double2hiint(res) + (int)((unsigned)e << 20), __double2loint(res));
 }
 
 template <typename R> __device__ __forceinline__ R cns_pow(R a, R b);
