@@ -73,34 +73,23 @@ __device__ __forceinline__ R d2x_nu(const Get& get, const R* __restrict__ cvsx, 
     return s;
 }
 
-// FP64 body: contribution of direction DIR (deviceRHSX/Y/Z) on the separate stencil fields,
-// the velocity gradients from the gradient kernel. The viscous momentum terms
-// (grad mu . s + mu lap u + mu/3 grad theta) of all directions are summed in W[] and the
-// dissipation / conduction in diss / cond, so the energy equation's u_i W_i work term
-// and the mu multiplications are applied once per point instead of once per direction.
+// FP64 body: contribution of direction DIR (deviceRHSX/Y/Z) on the separate stencil fields.
+// Terms that every direction multiplies by the same centre value are summed over the
+// directions first and multiplied once per point (rhs_point_nb): the second derivatives of
+// u, v, w, T in L[] (times mu), the viscous momentum terms grad mu . s + mu/3 grad theta in
+// W[] (the energy equation's work u_i W_i), the conduction in cond (times lambda/mu), and
+// the mass flux, whose half carries the centre value of the four cubic fluxes. The stress
+// row tau_{DIR,c}/mu comes from rhs_point_nb, which forms the symmetric tensor once.
 // (The FP32-RHS mode has its own body on the packed records, rhs_dir_packed below.)
 template <typename R, int S, int V, int DIR, class NB>
 __device__ __forceinline__ void rhs_direction(const Geom& g, const CoefT<R>& cf, const NB& nb, int i,
-                                              R (&Gr)[9], R th0, R m0, R m3, R u0, R v0, R w0, R r0, R h0,
-                                              int quirk, R (&acc)[5], R (&W)[3], R& diss, R& cond, R& dmu_dir) {
+                                              const R (&tau)[3], R m3, R u0, R v0, R w0, R r0, R (&acc)[5],
+                                              R (&W)[3], R (&L)[4], R& cond) {
     const bool nux = (DIR == 0) && g.nonuniform_x;
     const R xpi = nux ? cf.xp[i] : (R)1;
     const R* c1V = cf.c1V[DIR];
     const R* c1S = cf.c1S[DIR];
     const R* c2V = cf.c2V[DIR];
-
-    // stress row tau_{DIR, c} / mu  (uXtmp, vXtmp, wXtmp of deviceRHSX and its y/z twins)
-    R tau[3];
-    {
-#pragma unroll
-        for (int q = 0; q < 3; q++)
-            tau[q] = (q == DIR) ? (R)2 * Gr[3 * DIR + q] - (R)(2. / 3.) * th0 : Gr[3 * DIR + q] + Gr[3 * q + DIR];
-        // viscous dissipation tau_{DIR,c} d u_c / d x_DIR / mu (y: tau_yz dv/dz with the quirk, cuda_rhs.cu:175)
-        const R dw = (DIR == 1 && quirk) ? Gr[7] : Gr[3 * DIR + 2];
-        diss = fma(tau[0], Gr[3 * DIR + 0], diss);
-        diss = fma(tau[1], Gr[3 * DIR + 1], diss);
-        diss = fma(tau[2], dw, diss);
-    }
 
     // velocity stencils, loaded once for the viscous second derivatives and the fluxes
     R us[2 * S + 1], vs[2 * S + 1], ws[2 * S + 1];
@@ -111,43 +100,40 @@ __device__ __forceinline__ void rhs_direction(const Geom& g, const CoefT<R>& cf,
         vs[S + l] = nb.v(l); vs[S - l] = nb.v(-l);
         ws[S + l] = nb.w(l); ws[S - l] = nb.w(-l);
     }
-    // d mu/dx s_{DIR,c} + mu d2 u_c/dx2
+    // d mu/dx s_{DIR,c}; the second derivatives d2 u_c/dx2 continue the sums L[]
     const auto gm = [&](int l) { return nb.m(l); };
     const auto gt = [&](int l) { return nb.t(l); };
     const auto gd = [&](int l) { return nb.dil(l); };
     const auto gp = [&](int l) { return nb.p(l); };
     const R dmu = d1<R, V>(gm, c1V) * xpi;
-    dmu_dir = dmu;
-    R d2uu, d2vv, d2ww, d2tt;
     if (nux) {
-        R a = (R)0, b = (R)0, e2 = (R)0;
 #pragma unroll
         for (int it = 0; it < 2 * V + 1; it++) {
             const R cw = __ldg(cf.cvsx + it * g.mx + i);
-            a = fma(cw, us[S + it - V], a);
-            b = fma(cw, vs[S + it - V], b);
-            e2 = fma(cw, ws[S + it - V], e2);
+            L[0] = fma(cw, us[S + it - V], L[0]);
+            L[1] = fma(cw, vs[S + it - V], L[1]);
+            L[2] = fma(cw, ws[S + it - V], L[2]);
+            L[3] = fma(cw, nb.t(it - V), L[3]);
         }
-        d2uu = a; d2vv = b; d2ww = e2;
-        d2tt = d2x_nu<R, V>(gt, cf.cvsx, g.mx, i);
     } else {
-        R a = c2V[0] * us[S], b = c2V[0] * vs[S], e2 = c2V[0] * ws[S];
+        L[0] = fma(c2V[0], us[S], L[0]);
+        L[1] = fma(c2V[0], vs[S], L[1]);
+        L[2] = fma(c2V[0], ws[S], L[2]);
+        L[3] = fma(c2V[0], nb.t(0), L[3]);
 #pragma unroll
         for (int k = 1; k <= V; k++) {
-            a = fma(c2V[k], us[S + k] + us[S - k], a);
-            b = fma(c2V[k], vs[S + k] + vs[S - k], b);
-            e2 = fma(c2V[k], ws[S + k] + ws[S - k], e2);
+            L[0] = fma(c2V[k], us[S + k] + us[S - k], L[0]);
+            L[1] = fma(c2V[k], vs[S + k] + vs[S - k], L[1]);
+            L[2] = fma(c2V[k], ws[S + k] + ws[S - k], L[2]);
+            L[3] = fma(c2V[k], nb.t(k) + nb.t(-k), L[3]);
         }
-        d2uu = a; d2vv = b; d2ww = e2;
-        d2tt = d2u<R, V>(gt, c2V);
     }
-    W[0] = fma(tau[0], dmu, fma(d2uu, m0, W[0]));
-    W[1] = fma(tau[1], dmu, fma(d2vv, m0, W[1]));
-    W[2] = fma(tau[2], dmu, fma(d2ww, m0, W[2]));
-    // heat conduction lambda d2T + dlambda dT = (lambda/mu) (mu d2T + dmu dT); the ratio
-    // is applied once per point
+    W[0] = fma(tau[0], dmu, W[0]);
+    W[1] = fma(tau[1], dmu, W[1]);
+    W[2] = fma(tau[2], dmu, W[2]);
+    // heat conduction lambda d2T + dlambda dT = (lambda/mu) (mu d2T + dmu dT); mu d2T and
+    // the ratio are applied once per point
     const R dt = d1<R, V>(gt, c1V) * xpi;
-    cond = fma(d2tt, m0, cond);
     cond = fma(dt, dmu, cond);
     // mu/3 d(theta) on the DIR momentum (and its work), pressure gradient
     const R dth = d1<R, V>(gd, c1V) * xpi;
@@ -161,7 +147,8 @@ __device__ __forceinline__ void rhs_direction(const Geom& g, const CoefT<R>& cf,
     //   sum_l a_l [Q-(phi_{-l}+phi_0) - Q+(phi_0+phi_l)]
     //     = sum_l [(a_l Q-) phi_{-l} - (a_l Q+) phi_l]  +  phi_0 sum_l a_l (Q- - Q+),
     // and the last sum is half the mass flux (fq = 2 fc), so the products a_l Q+- are
-    // shared by the four cubic fluxes: 18 instead of 28 operations per l.
+    // shared by the four cubic fluxes: 18 instead of 28 operations per l. The phi_0 terms of
+    // all directions are added from the summed mass flux once per point.
     const R un = DIR == 0 ? u0 : (DIR == 1 ? v0 : w0);
     R sq = (R)0, fu = nux ? (R)0 : acc[1], fv = nux ? (R)0 : acc[2], fw = nux ? (R)0 : acc[3],
       fe = nux ? (R)0 : acc[4];
@@ -185,11 +172,6 @@ __device__ __forceinline__ void rhs_direction(const Geom& g, const CoefT<R>& cf,
         fw = fma(am, wm, fma(-ap, wp, fw));
         fe = fma(am, hm, fma(-ap, hp, fe));
     }
-    const R half = (R)0.5 * sq;
-    fu = fma(u0, half, fu);
-    fv = fma(v0, half, fv);
-    fw = fma(w0, half, fw);
-    fe = fma(h0, half, fe);
     const R fr = nux ? sq : acc[0] + sq;
     if (nux) {
         acc[0] = fma(xpi, fr, acc[0]);
@@ -250,11 +232,21 @@ __device__ __forceinline__ void stage_tail(const Geom& g, const Update<R>& up, d
 #pragma unroll
             for (int q = 0; q < 5; q++) prev[q] = up.rb[q][c];
         }
+        if constexpr (sizeof(R) == 8) {
+            // q0 + dt (a prev + b acc) with dt a, dt b formed once: two operations per field
+            const double dta = dt * a, dtb = dt * b;
 #pragma unroll
-        for (int q = 0; q < 5; q++) {
-            const R x = up.use_prev ? fma(a, prev[q], b * acc[q]) : b * acc[q];
-            qn[q] = fma(dt, to_d<R>(x), q0[q]);
-            up.rb[q][c] = acc[q];
+            for (int q = 0; q < 5; q++) {
+                qn[q] = fma(dtb, acc[q], up.use_prev ? fma(dta, prev[q], q0[q]) : q0[q]);
+                up.rb[q][c] = acc[q];
+            }
+        } else {
+#pragma unroll
+            for (int q = 0; q < 5; q++) {
+                const R x = up.use_prev ? fma(a, prev[q], b * acc[q]) : b * acc[q];
+                qn[q] = fma(dt, to_d<R>(x), q0[q]);
+                up.rb[q][c] = acc[q];
+            }
         }
     } else if (up.kind == ST_C1 || up.kind == ST_R4_1) {
         const double q0[5] = {rr, rr * uu, rr * vv, rr * ww, ee};
@@ -306,17 +298,36 @@ __device__ __forceinline__ void rhs_point_nb(const Geom& g, const CoefT<R>& cf, 
                                              const Update<R>& up, double* __restrict__ scal, int quirk, int i,
                                              int k, int c, const NX& nx, const NY& ny, const NZ& nz, R th0,
                                              R m0, R u0, R v0, R w0, R r0, R h0) {
-    R Gr[9];   // the gradient kernel's fields
+    R Gr[9];   // the gradient kernel's fields, Gr[3 a + b] = d u_b / d x_a
 #pragma unroll
     for (int q = 0; q < 9; q++) Gr[q] = ld(in.g[q], c);
+    // the stress tensor tau / mu (uXtmp, vXtmp, wXtmp of deviceRHSX and its y/z twins) and
+    // the viscous dissipation tau_ab d u_b / d x_a / mu; an off-diagonal pair contributes
+    // tau_ab (d u_b/d x_a + d u_a/d x_b) = tau_ab^2, except y-z with the quirk
+    // (cuda_rhs.cu:175: tau_yz dv/dz in the y sum as in the z sum)
+    const R th23 = (R)(2. / 3.) * th0;
+    const R t00 = fma((R)2, Gr[0], -th23), t11 = fma((R)2, Gr[4], -th23), t22 = fma((R)2, Gr[8], -th23);
+    const R t01 = Gr[1] + Gr[3], t02 = Gr[2] + Gr[6], t12 = Gr[5] + Gr[7];
+    const R q12 = quirk ? Gr[7] + Gr[7] : t12;
+    const R diss = fma(t00, Gr[0], fma(t11, Gr[4], fma(t22, Gr[8], fma(t01, t01, fma(t02, t02, t12 * q12)))));
+    const R tx[3] = {t00, t01, t02}, ty[3] = {t01, t11, t12}, tz[3] = {t02, t12, t22};
     const R m3 = m0 * (R)(1.0 / 3.0);
     R acc[5] = {0, 0, 0, 0, 0};
     R W[3] = {0, 0, 0};
-    R diss = 0, cond = 0;
-    R dmu[3];
-    rhs_direction<R, S, V, 0>(g, cf, nx, i, Gr, th0, m0, m3, u0, v0, w0, r0, h0, quirk, acc, W, diss, cond, dmu[0]);
-    rhs_direction<R, S, V, 1>(g, cf, ny, i, Gr, th0, m0, m3, u0, v0, w0, r0, h0, quirk, acc, W, diss, cond, dmu[1]);
-    rhs_direction<R, S, V, 2>(g, cf, nz, i, Gr, th0, m0, m3, u0, v0, w0, r0, h0, quirk, acc, W, diss, cond, dmu[2]);
+    R L[4] = {0, 0, 0, 0};
+    R cond = 0;
+    rhs_direction<R, S, V, 0>(g, cf, nx, i, tx, m3, u0, v0, w0, r0, acc, W, L, cond);
+    rhs_direction<R, S, V, 1>(g, cf, ny, i, ty, m3, u0, v0, w0, r0, acc, W, L, cond);
+    rhs_direction<R, S, V, 2>(g, cf, nz, i, tz, m3, u0, v0, w0, r0, acc, W, L, cond);
+    // the centre values of the cubic fluxes: phi_0 times half the mass flux
+    const R half = (R)0.5 * acc[0];
+    acc[1] = fma(u0, half, acc[1]);
+    acc[2] = fma(v0, half, acc[2]);
+    acc[3] = fma(w0, half, acc[3]);
+    acc[4] = fma(h0, half, acc[4]);
+#pragma unroll
+    for (int q = 0; q < 3; q++) W[q] = fma(m0, L[q], W[q]);
+    cond = fma(m0, L[3], cond);
     acc[1] += W[0];
     acc[2] += W[1];
     acc[3] += W[2];
