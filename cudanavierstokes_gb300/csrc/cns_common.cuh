@@ -162,6 +162,13 @@ __device__ __forceinline__ double rcp_nr(double x) {
     return fma(r, fma(e, e, e), r);
 }
 
+// x > 0 (NaN excluded) from the IEEE bit pattern, on the integer units: the patterns of
+// +denormals .. +infinity are the signed 64-bit integers in (0, 0x7ff0000000000000]
+__device__ __forceinline__ bool positive_bits(double x) {
+    const long long b = __double_as_longlong(x);
+    return b > 0 && b <= 0x7ff0000000000000LL;
+}
+
 // x^a in FP64 for the viscosity law mu ~ T^a, as exp(a ln x) with 64-entry tables
 // (pow_tables.h, generated with 60-digit arithmetic by gen_pow_tables.py):
 //   ln x = k ln2 - ln r_i + ln(1 + d),  x = 2^k m,  m in [1, 2),  i = the top 6 fraction

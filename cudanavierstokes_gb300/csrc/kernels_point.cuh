@@ -34,16 +34,19 @@ __device__ __forceinline__ void state_store(const Phys& ph, const DerivedOut<R>&
         // the positivity test on the FP32 roundings keeps it off the FP64 pipe
         if (!(Tf > 0.f) || !(rf > 0.f)) scal[SC_NONFINITE] = 1.0;   // racy flag write, any writer is fine
     } else {
-        const double en = ee * inv - 0.5 * (uu * uu + vv * vv + ww * ww);
-        const double T = ph.cvInv * en;
-        const double pr = rr * ph.Rgas * T;
-        const double hh = (ee + pr) * inv;
+        // R T shared by p = rho (R T) and H = E/rho + R T (= (rhoE + p)/rho); the positivity
+        // test on the bit patterns (integer units)
+        const double er = ee * inv;
+        const double T = ph.cvInv * fma(-0.5, uu * uu + vv * vv + ww * ww, er);
+        const double RT = ph.Rgas * T;
+        const double pr = rr * RT;
+        const double hh = er + RT;
         o.t[c] = T;
         o.p[c] = pr;
         o.h[c] = hh;
         const double suth = ph.vexp_is_one ? T : pow_visc(T, ph.vexp);
         o.m[c] = (R)(suth * ph.invRe);
-        if (!(T > 0.0) || !(rr > 0.0)) scal[SC_NONFINITE] = 1.0;   // racy flag write, any writer is fine
+        if (!positive_bits(T) || !positive_bits(rr)) scal[SC_NONFINITE] = 1.0;   // racy flag write, any writer is fine
     }
 }
 

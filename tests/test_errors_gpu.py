@@ -28,6 +28,21 @@ def test_negative_temperature_is_rejected_at_copy_in(gpu_lib, prec):
 
 
 @pytest.mark.parametrize("prec", [PREC_FP64, PREC_FP32_RHS])
+@pytest.mark.parametrize("bad", [0.0, -0.0, -1.0, float("nan"), float("-nan")])
+def test_non_positive_density_is_rejected_at_copy_in(gpu_lib, prec, bad):
+    """The positivity test of the recovered state (on the bit patterns in FP64 mode) flags
+    zero of either sign, negative and NaN densities."""
+    p = tgv_params(16, precision=prec)
+    r, u, v, w, e = tgv_fields(p)
+    r = r.copy()
+    r[2, 7, 1] = bad
+    s = Solver(p)
+    with pytest.raises(CnsError) as ei:
+        s.copy_field_in(r, u, v, w, e)
+    assert ei.value.code == CNS_ERR_NONFINITE
+
+
+@pytest.mark.parametrize("prec", [PREC_FP64, PREC_FP32_RHS])
 def test_unstable_run_reports_nonfinite_state(gpu_lib, prec):
     p = tgv_params(16, precision=prec).copy(cfl=50.0)
     s = Solver(p)
