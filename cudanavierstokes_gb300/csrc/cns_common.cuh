@@ -11,6 +11,7 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include "ff.cuh"
 #include "pow_tables.h"
 
 namespace cns {
@@ -141,11 +142,15 @@ __device__ __forceinline__ double f2d(float f) {
 // conversions between FP64 and the arithmetic type R of a kernel
 template <typename R>
 __device__ __forceinline__ R to_r(double x) {
-    if constexpr (sizeof(R) == 4) return d2f(x); else return x;
+    if constexpr (sizeof(R) == 4) return d2f(x);
+    else if constexpr (is_ff<R>) return d_to_ff(x);
+    else return x;
 }
 template <typename R>
 __device__ __forceinline__ double to_d(R x) {
-    if constexpr (sizeof(R) == 4) return f2d(x); else return x;
+    if constexpr (sizeof(R) == 4) return f2d(x);
+    else if constexpr (is_ff<R>) return ff_to_d(x);
+    else return x;
 }
 
 // Reciprocal of a double from an FP32 seed r0 (|e| <= ~2^-23 with e = 1 - x r0):

@@ -27,6 +27,7 @@ struct StateOut {
 template <typename R>
 struct DerivedOut {
     R *h, *t, *p, *m;   // FP64 mode
+    R *r, *u, *v, *w;   // pair mode: the state's rho, u, v, w as pairs
     float4 *qa, *qb;    // FP32-RHS mode
 };
 
@@ -119,5 +120,7 @@ int launch_rhs_fp64(int S, int V, const Geom& g, const Phys& ph, const CoefT<dou
                     const Update<double>& up, double* scal, int quirk, cudaStream_t s);
 int launch_rhs_fp32(int S, int V, const Geom& g, const Phys& ph, const CoefT<float>& cf, const RhsIn<float>& in,
                     const Update<float>& up, double* scal, int quirk, cudaStream_t s);
+int launch_rhs_pair(int S, int V, const Geom& g, const Phys& ph, const CoefT<ff>& cf, const RhsIn<ff>& in,
+                    const Update<ff>& up, double* scal, int quirk, cudaStream_t s);
 
 }  // namespace cns

@@ -1,0 +1,91 @@
+// ff.cuh -- double-float ("FP32 pair") arithmetic: a value is the unevaluated sum h + l of
+// two FP32 numbers with |l| <= ulp(h)/2, about 48 significant bits (relative precision
+// ~2^-48 against FP64's 2^-53) in FP32's exponent range.
+//
+// The operations are the double-word algorithms of Joldes, Muller and Popescu, "Tight and
+// rigorous error bounds for basic building blocks of double-word arithmetic" (ACM TOMS 44,
+// 2017), built on Knuth's 2Sum, Dekker's Fast2Sum and the FMA-based exact product:
+//   +  "SloppyDWPlusDW" (Alg. 5, 11 FP32 operations): error <= ~u^2 (|x| + |y|), u = 2^-24,
+//      the norm-wise bound of an FP64 sum with u^2 in place of 2^-53;
+//   *  "DWTimesDW" (Alg. 12, 9 operations): relative error <= 5 u^2.
+// Every step uses the _rn intrinsics, which the compiler neither contracts into FMAs nor
+// reassociates: the error-free transforms rely on each rounding happening as written.
+//
+// On this GPU an FP64 operation issues to 2 lanes per SM per cycle and an FP32 one to 128,
+// so a pair operation of 9-20 FP32 instructions still has several times the FP64 rate.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <type_traits>
+
+namespace cns {
+
+struct ff {
+    float h, l;
+    ff() = default;
+    __host__ __device__ constexpr ff(float a, float b) : h(a), l(b) {}
+    // from an integer constant (0, 1, 2 in generic code); a template, so that no double
+    // reaches it through a conversion to int
+    template <typename I, typename std::enable_if<std::is_integral<I>::value, int>::type = 0>
+    __host__ __device__ constexpr ff(I x) : h((float)x), l(0.0f) {}
+    // nearest pair to a double (compile-time constants fold; at run time two conversions
+    // and one FP64 subtraction)
+    __host__ __device__ explicit constexpr ff(double x) : h((float)x), l((float)(x - (double)(float)x)) {}
+};
+
+__device__ __forceinline__ ff fast_two_sum(float a, float b) {   // |a| >= |b| or a = 0
+    const float s = __fadd_rn(a, b);
+    return ff(s, __fsub_rn(b, __fsub_rn(s, a)));
+}
+
+__device__ __forceinline__ ff two_sum(float a, float b) {
+    const float s = __fadd_rn(a, b);
+    const float bb = __fsub_rn(s, a);
+    const float e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
+    return ff(s, e);
+}
+
+__device__ __forceinline__ ff operator+(ff x, ff y) {
+    const ff s = two_sum(x.h, y.h);
+    const float w = __fadd_rn(s.l, __fadd_rn(x.l, y.l));
+    return fast_two_sum(s.h, w);
+}
+
+__device__ __forceinline__ ff operator-(ff x) { return ff(-x.h, -x.l); }
+__device__ __forceinline__ ff operator-(ff x, ff y) { return x + ff(-y.h, -y.l); }
+
+__device__ __forceinline__ ff operator*(ff x, ff y) {
+    const float ch = __fmul_rn(x.h, y.h);
+    const float cl1 = __fmaf_rn(x.h, y.h, -ch);
+    const float tl1 = __fmaf_rn(x.h, y.l, __fmul_rn(x.l, y.l));
+    const float cl2 = __fmaf_rn(x.l, y.h, tl1);
+    return fast_two_sum(ch, __fadd_rn(cl1, cl2));
+}
+
+// the pair overload joins the FP32 / FP64 ones (a namespace-scope fma would hide them)
+using ::fma;
+__device__ __forceinline__ ff fma(ff a, ff b, ff c) { return a * b + c; }
+
+__device__ __forceinline__ ff& operator+=(ff& a, ff b) { a = a + b; return a; }
+__device__ __forceinline__ ff& operator-=(ff& a, ff b) { a = a - b; return a; }
+__device__ __forceinline__ ff& operator*=(ff& a, ff b) { a = a * b; return a; }
+
+template <typename R>
+inline constexpr bool is_ff = false;
+template <>
+inline constexpr bool is_ff<ff> = true;
+
+// FP64 <-> pair: h + l in FP64 is exact (48 bits); the split rounds h, then the remainder
+__device__ __forceinline__ double ff_to_d(ff x) { return (double)x.h + (double)x.l; }
+__device__ __forceinline__ ff d_to_ff(double x) {
+    const float h = __double2float_rn(x);
+    return ff(h, __double2float_rn(x - (double)h));
+}
+
+}  // namespace cns
+
+// read-only cached load of a pair (one 8-byte load)
+__device__ __forceinline__ cns::ff __ldg(const cns::ff* p) {
+    const float2 v = __ldg(reinterpret_cast<const float2*>(p));
+    return cns::ff(v.x, v.y);
+}

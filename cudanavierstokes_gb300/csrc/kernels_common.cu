@@ -188,7 +188,9 @@ __global__ void __launch_bounds__(256) k_pack(Geom g, const T* __restrict__ src,
     const unsigned mx = (unsigned)g.mx, my = (unsigned)g.my;
     for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x) {
         const unsigned tt = (unsigned)t, jk = tt / mx;
-        dst[t] = (double)src[g.at((int)(tt - jk * mx), (int)(jk % my), (int)(jk / my))];
+        const T x = src[g.at((int)(tt - jk * mx), (int)(jk % my), (int)(jk / my))];
+        if constexpr (is_ff<T>) dst[t] = ff_to_d(x);
+        else dst[t] = (double)x;
     }
 }
 
@@ -269,5 +271,15 @@ CNS_INST(double)
 CNS_INST(float)
 template void launch_grad<double>(int, const Geom&, const CoefT<double>&, const double*, const double*, const double*,
                                   const GradOut<double>&, int, cudaStream_t);
+// pair mode (FP32-pair RHS arithmetic): the stencil-input kernels and the RHS output
+template void launch_state<ff>(const Geom&, const Phys&, const StateIn&, const DerivedOut<ff>&, double*, int, double*,
+                               long long, cudaStream_t);
+template void launch_ghost_state<ff>(const Geom&, const Phys&, const StencilFields<ff>&, const double*, cudaStream_t);
+template void launch_ghost_scalar<ff>(const Geom&, ff*, cudaStream_t);
+template int launch_reduce<ff>(const Geom&, const Phys&, const StateIn&, const ff*, int, double*, int, double*, double*,
+                               cudaStream_t);
+template void launch_pack<ff>(const Geom&, const ff*, double*, cudaStream_t);
+template void launch_grad<ff>(int, const Geom&, const CoefT<ff>&, const ff*, const ff*, const ff*, const GradOut<ff>&,
+                              int, cudaStream_t);
 
 }  // namespace cns

@@ -41,11 +41,17 @@ __device__ __forceinline__ void state_store(const Phys& ph, const DerivedOut<R>&
         const double RT = ph.Rgas * T;
         const double pr = rr * RT;
         const double hh = er + RT;
-        o.t[c] = T;
-        o.p[c] = pr;
-        o.h[c] = hh;
         const double suth = ph.vexp_is_one ? T : pow_visc(T, ph.vexp);
-        o.m[c] = (R)(suth * ph.invRe);
+        if constexpr (is_ff<R>) {   // the pair mode's stencil inputs include rho, u, v, w
+            o.r[c] = d_to_ff(rr);
+            o.u[c] = d_to_ff(uu);
+            o.v[c] = d_to_ff(vv);
+            o.w[c] = d_to_ff(ww);
+        }
+        o.t[c] = to_r<R>(T);
+        o.p[c] = to_r<R>(pr);
+        o.h[c] = to_r<R>(hh);
+        o.m[c] = to_r<R>(suth * ph.invRe);
         if (!positive_bits(T) || !positive_bits(rr)) scal[SC_NONFINITE] = 1.0;   // racy flag write, any writer is fine
     }
 }
@@ -204,33 +210,36 @@ __device__ __forceinline__ void ghost_state_cell(const Geom& g, const Phys& ph, 
         const int j = gc.j, k = gc.k;
         cg = g.at(side == 0 ? -m : g.mx - 1 + m, j, k);
         if (g.xbc != XBC_PER) {
+            // in FP64 (the pair mode converts the interior values and the results)
             const long long cp = g.at(side == 0 ? m - 1 : g.mx - m, j, k);
-            R ug, vg, wg, pg, Tg;
+            const auto rd = [&](const R* a, long long e) { return to_d<R>(a[e]); };
+            double ug, vg, wg, pg, Tg;
             if (g.xbc == XBC_WALL) {
                 const double Tw = side == 0 ? ph.twall_bot : ph.twall_top;
-                ug = -f.u[cp]; vg = -f.v[cp]; wg = -f.w[cp];
-                pg = f.p[cp];
-                Tg = (R)(2.0 * Tw) - f.t[cp];
+                ug = -rd(f.u, cp); vg = -rd(f.v, cp); wg = -rd(f.w, cp);
+                pg = rd(f.p, cp);
+                Tg = 2.0 * Tw - rd(f.t, cp);
             } else if (side == 0) {   // boundary layer, wall
-                ug = -f.u[cp]; vg = -f.v[cp]; wg = -f.w[cp];
-                pg = f.p[cp];
-                Tg = f.t[cp];
+                ug = -rd(f.u, cp); vg = -rd(f.v, cp); wg = -rd(f.w, cp);
+                pg = rd(f.p, cp);
+                Tg = rd(f.t, cp);
                 double pv;
-                if (ph.perturbed && wall_perturbation(ph, g.dy, j, k, scal[SC_TIME], &pv)) ug = to_r<R>(pv);
+                if (ph.perturbed && wall_perturbation(ph, g.dy, j, k, scal[SC_TIME], &pv)) ug = pv;
             } else {                  // boundary layer, free stream: extrapolate through the last node
                 const long long cl = g.at(g.mx - 1, j, k);
                 const long long cm = g.at(g.mx - 1 - m, j, k);
-                ug = (R)2.0 * f.u[cl] - f.u[cm];
-                vg = (R)2.0 * f.v[cl] - f.v[cm];
-                wg = (R)2.0 * f.w[cl] - f.w[cm];
-                pg = (R)2.0 * f.p[cl] - f.p[cm];
-                Tg = (R)2.0 * f.t[cl] - f.t[cm];
+                ug = 2.0 * rd(f.u, cl) - rd(f.u, cm);
+                vg = 2.0 * rd(f.v, cl) - rd(f.v, cm);
+                wg = 2.0 * rd(f.w, cl) - rd(f.w, cm);
+                pg = 2.0 * rd(f.p, cl) - rd(f.p, cm);
+                Tg = 2.0 * rd(f.t, cl) - rd(f.t, cm);
             }
-            const R suth = ph.vexp_is_one ? Tg : cns_pow<R>(Tg, (R)ph.vexp);
-            f.u[cg] = ug; f.v[cg] = vg; f.w[cg] = wg; f.p[cg] = pg; f.t[cg] = Tg;
-            f.m[cg] = suth * (R)ph.invRe;
-            f.h[cg] = Tg * (R)ph.hcoef + (R)0.5 * (ug * ug + vg * vg + wg * wg);
-            f.r[cg] = pg / ((R)ph.Rgas * Tg);
+            const double suth = ph.vexp_is_one ? Tg : cns_pow<double>(Tg, ph.vexp);
+            f.u[cg] = to_r<R>(ug); f.v[cg] = to_r<R>(vg); f.w[cg] = to_r<R>(wg); f.p[cg] = to_r<R>(pg);
+            f.t[cg] = to_r<R>(Tg);
+            f.m[cg] = to_r<R>(suth * ph.invRe);
+            f.h[cg] = to_r<R>(Tg * ph.hcoef + 0.5 * (ug * ug + vg * vg + wg * wg));
+            f.r[cg] = to_r<R>(pg / (ph.Rgas * Tg));
             return;
         }
         cs = g.at(side == 0 ? g.mx - m : m - 1, j, k);

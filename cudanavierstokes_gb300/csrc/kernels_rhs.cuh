@@ -201,12 +201,13 @@ __device__ __forceinline__ void stage_tail(const Geom& g, const Update<R>& up, d
     if (up.spx) {
         const R sg = to_r<R>(up.spx[i] + up.spz[k]);
         const long long i2 = (long long)i + (long long)k * g.mx;
-        if constexpr (sizeof(R) == 8) {
-            acc[0] += sg * (up.rref[i2] - rr);
-            acc[1] += sg * (up.uref[i2] - rr * uu);
-            acc[2] += sg * (up.vref[i2] - rr * vv);
-            acc[3] += sg * (up.wref[i2] - rr * ww);
-            acc[4] += sg * (up.eref[i2] - ee);
+        if constexpr (sizeof(R) == 8) {   // FP64 (and the pair type: the term in FP64, then split)
+            const double sgd = up.spx[i] + up.spz[k];
+            acc[0] += to_r<R>(sgd * (up.rref[i2] - rr));
+            acc[1] += to_r<R>(sgd * (up.uref[i2] - rr * uu));
+            acc[2] += to_r<R>(sgd * (up.vref[i2] - rr * vv));
+            acc[3] += to_r<R>(sgd * (up.wref[i2] - rr * ww));
+            acc[4] += to_r<R>(sgd * (up.eref[i2] - ee));
         } else {
             acc[0] += sg * (to_r<R>(up.rref[i2]) - r0);
             acc[1] += sg * (to_r<R>(up.uref[i2]) - r0 * u0);
@@ -236,10 +237,10 @@ __device__ __forceinline__ void stage_tail(const Geom& g, const Update<R>& up, d
         }
         if constexpr (sizeof(R) == 8) {
             // q0 + dt (a prev + b acc) with dt a, dt b formed once: two operations per field
-            const double dta = dt * a, dtb = dt * b;
+            const double dta = dt * up.a, dtb = dt * up.b;
 #pragma unroll
             for (int q = 0; q < 5; q++) {
-                qn[q] = fma(dtb, acc[q], up.use_prev ? fma(dta, prev[q], q0[q]) : q0[q]);
+                qn[q] = fma(dtb, to_d<R>(acc[q]), up.use_prev ? fma(dta, to_d<R>(prev[q]), q0[q]) : q0[q]);
                 up.rb[q][c] = acc[q];
             }
         } else {

@@ -94,7 +94,7 @@ int check_params(const cns_params* p) {
         return fail(CNS_ERR_INVALID, "Re, Pr, Ma, cfl must be > 0 and gam > 1");
     if (p->scheme < CNS_RK3_LOWSTORAGE || p->scheme > CNS_RK4_CLASSIC)
         return fail(CNS_ERR_INVALID, "unknown scheme %d", p->scheme);
-    if (p->precision != CNS_PREC_FP64 && p->precision != CNS_PREC_FP32_RHS)
+    if (p->precision != CNS_PREC_FP64 && p->precision != CNS_PREC_FP32_RHS && p->precision != CNS_PREC_PAIR_RHS)
         return fail(CNS_ERR_INVALID, "unknown precision %d", p->precision);
     if (p->check_cfl < 1 || p->check_bulk < 1) return fail(CNS_ERR_INVALID, "check_cfl and check_bulk must be >= 1");
     if (p->boundary_layer && p->periodic_x)
@@ -110,7 +110,13 @@ RhsIn<R> rhs_in(cns_solver* h, int c) {
         in.qa = (const float4*)h->der[c][0];
         in.qb = (const float4*)h->der[c][1];
     } else {
-        in.r = (const R*)h->q[c][0]; in.u = (const R*)h->q[c][1]; in.v = (const R*)h->q[c][2]; in.w = (const R*)h->q[c][3];
+        if constexpr (is_ff<R>) {   // rho, u, v, w as pairs, written by the state recovery
+            in.r = (const R*)h->der[c][4]; in.u = (const R*)h->der[c][5]; in.v = (const R*)h->der[c][6];
+            in.w = (const R*)h->der[c][7];
+        } else {
+            in.r = (const R*)h->q[c][0]; in.u = (const R*)h->q[c][1]; in.v = (const R*)h->q[c][2];
+            in.w = (const R*)h->q[c][3];
+        }
         in.h = (const R*)h->der[c][0]; in.t = (const R*)h->der[c][1]; in.p = (const R*)h->der[c][2];
         in.m = (const R*)h->der[c][3];
         for (int q = 0; q < 9; q++) in.g[q] = (const R*)h->grad[q];
@@ -132,6 +138,9 @@ DerivedOut<R> derived_out(cns_solver* h, int b) {
         o.qb = (float4*)h->der[b][1];
     } else {
         o.h = (R*)h->der[b][0]; o.t = (R*)h->der[b][1]; o.p = (R*)h->der[b][2]; o.m = (R*)h->der[b][3];
+        if constexpr (is_ff<R>) {
+            o.r = (R*)h->der[b][4]; o.u = (R*)h->der[b][5]; o.v = (R*)h->der[b][6]; o.w = (R*)h->der[b][7];
+        }
     }
     return o;
 }
@@ -156,6 +165,9 @@ int ghost_phase(cns_solver* h) {
     StencilFields<R> f{};
     if (h->fp32) {
         f.qa = o.qa; f.qb = o.qb;
+    } else if constexpr (is_ff<R>) {
+        f.r = o.r; f.u = o.u; f.v = o.v; f.w = o.w;
+        f.t = o.t; f.p = o.p; f.h = o.h; f.m = o.m;
     } else {
         f.r = (R*)h->q[c][0]; f.u = (R*)h->q[c][1]; f.v = (R*)h->q[c][2]; f.w = (R*)h->q[c][3];
         f.t = o.t; f.p = o.p; f.h = o.h; f.m = o.m;
@@ -178,10 +190,11 @@ int grad_phase(cns_solver* h) {
         GradOut<R> o;
         for (int q = 0; q < 9; q++) o.g[q] = (R*)h->grad[q];
         o.dil = (R*)h->dil;
-        const R* u = (const R*)h->q[h->cur][1];
-        const R* v = (const R*)h->q[h->cur][2];
-        const R* w = (const R*)h->q[h->cur][3];
-        launch_grad<R>(h->p.stencil_visc, h->geom, h->cf64, u, v, w, o, own ? 1 : 0, h->stream);
+        const RhsIn<R> in = rhs_in<R>(h, h->cur);
+        if constexpr (is_ff<R>)
+            launch_grad<R>(h->p.stencil_visc, h->geom, h->cfp, in.u, in.v, in.w, o, own ? 1 : 0, h->stream);
+        else
+            launch_grad<R>(h->p.stencil_visc, h->geom, h->cf64, in.u, in.v, in.w, o, own ? 1 : 0, h->stream);
     }
     h->launches += 1;
     if (!own) {
@@ -200,8 +213,8 @@ Update<R> stage_update(cns_solver* h, int kind, double a, double b, int c, bool 
     up.kind = kind;
     up.a = a;
     up.b = b;
-    up.ca = (R)a;
-    up.cb = (R)b;
+    up.ca = R(a);
+    up.cb = R(b);
     up.use_prev = a != 0.0;
     up.qin = state_in(h, c);
     const int nb = 1 - c;
@@ -232,6 +245,9 @@ int rhs_phase(cns_solver* h, int kind, double a, double b) {
     if constexpr (std::is_same<R, float>::value)
         nl = launch_rhs_fp32(h->p.stencil_size, h->p.stencil_visc, h->geom, h->phys, h->cf32, rhs_in<float>(h, h->cur),
                              up, h->scal, quirk, h->stream);
+    else if constexpr (is_ff<R>)
+        nl = launch_rhs_pair(h->p.stencil_size, h->p.stencil_visc, h->geom, h->phys, h->cfp, rhs_in<ff>(h, h->cur),
+                             up, h->scal, quirk, h->stream);
     else
         nl = launch_rhs_fp64(h->p.stencil_size, h->p.stencil_visc, h->geom, h->phys, h->cf64,
                              rhs_in<double>(h, h->cur), up, h->scal, quirk, h->stream);
@@ -247,13 +263,20 @@ int rhs_phase(cns_solver* h, int kind, double a, double b) {
     return CNS_OK;
 }
 
-int state_any(cns_solver* h) { return h->fp32 ? state_phase<float>(h) : state_phase<double>(h); }
-int ghost_any(cns_solver* h) { return h->fp32 ? ghost_phase<float>(h) : ghost_phase<double>(h); }
+int state_any(cns_solver* h) {
+    return h->fp32 ? state_phase<float>(h) : h->pair ? state_phase<ff>(h) : state_phase<double>(h);
+}
+int ghost_any(cns_solver* h) {
+    return h->fp32 ? ghost_phase<float>(h) : h->pair ? ghost_phase<ff>(h) : ghost_phase<double>(h);
+}
 // the derived fields of the current state, recovered unless the last stage did it
 int ensure_state(cns_solver* h) { return h->der_ok[h->cur] ? CNS_OK : state_any(h); }
-int grad_any(cns_solver* h) { return h->fp32 ? grad_phase<float>(h) : grad_phase<double>(h); }
+int grad_any(cns_solver* h) {
+    return h->fp32 ? grad_phase<float>(h) : h->pair ? grad_phase<ff>(h) : grad_phase<double>(h);
+}
 int rhs_any(cns_solver* h, int kind, double a, double b) {
-    return h->fp32 ? rhs_phase<float>(h, kind, a, b) : rhs_phase<double>(h, kind, a, b);
+    return h->fp32 ? rhs_phase<float>(h, kind, a, b)
+                   : h->pair ? rhs_phase<ff>(h, kind, a, b) : rhs_phase<double>(h, kind, a, b);
 }
 
 }  // namespace
@@ -276,6 +299,9 @@ int cns::solver_reduce(cns_solver* h, int want, double* diag) {
     if (h->fp32)   // mu is the fourth value of the packed record (T, p, H, mu)
         launch_reduce<float>(h->geom, h->phys, state_in(h, h->cur), (const float*)h->der[h->mu_buf][1] + 3, 4, h->part,
                              want, h->scal, diag, h->stream);
+    else if (h->pair)
+        launch_reduce<ff>(h->geom, h->phys, state_in(h, h->cur), (const ff*)h->der[h->mu_buf][3], 1, h->part, want,
+                          h->scal, diag, h->stream);
     else launch_reduce<double>(h->geom, h->phys, state_in(h, h->cur), (const double*)h->der[h->mu_buf][3], 1, h->part,
                                want, h->scal, diag, h->stream);
     h->launches += 2;
@@ -356,9 +382,15 @@ int upload_grid_tables(cns_solver* h) {
     int rc;
     if ((rc = h->alloc(&h->xp_d, mx)) || (rc = h->alloc(&h->wvol_d, mx)) || (rc = h->alloc(&h->dxv_d, mx)) ||
         (rc = h->alloc(&h->cvsx_d, (size_t)mx * (2 * V + 1))) || (rc = h->alloc(&h->xp_f, mx)) ||
-        (rc = h->alloc(&h->cvsx_f, (size_t)mx * (2 * V + 1))))
+        (rc = h->alloc(&h->cvsx_f, (size_t)mx * (2 * V + 1))) || (rc = h->alloc(&h->xp_p, mx)) ||
+        (rc = h->alloc(&h->cvsx_p, (size_t)mx * (2 * V + 1))))
         return rc;
     std::vector<float> xpf(g.xp.begin(), g.xp.end()), cvf(g.cvsx.begin(), g.cvsx.end());
+    std::vector<ff> xpp, cvp;
+    for (double v : g.xp) xpp.push_back(ff(v));
+    for (double v : g.cvsx) cvp.push_back(ff(v));
+    CK(cudaMemcpy(h->xp_p, xpp.data(), mx * sizeof(ff), cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(h->cvsx_p, cvp.data(), cvp.size() * sizeof(ff), cudaMemcpyHostToDevice));
     CK(cudaMemcpy(h->xp_d, g.xp.data(), mx * sizeof(double), cudaMemcpyHostToDevice));
     CK(cudaMemcpy(h->wvol_d, g.wvol.data(), mx * sizeof(double), cudaMemcpyHostToDevice));
     CK(cudaMemcpy(h->dxv_d, g.dxv.data(), mx * sizeof(double), cudaMemcpyHostToDevice));
@@ -435,7 +467,8 @@ int cns_create(const cns_params* pin, int device, cns_solver** out) {
     h->p = *pin;
     h->device = device;
     h->fp32 = pin->precision == CNS_PREC_FP32_RHS;
-    h->rsz = h->fp32 ? 4 : 8;
+    h->pair = pin->precision == CNS_PREC_PAIR_RHS;
+    h->rsz = h->fp32 ? 4 : 8;   // FP64 and pairs: 8 bytes
     const cns_params& p = h->p;
     const int S = p.stencil_size, G = S;
     build_grid(p, h->hg);
@@ -490,6 +523,18 @@ int cns_create(const cns_params* pin, int device, cns_solver** out) {
         h->cf64.inv[d] = inv[d]; h->cf64.inv2[d] = inv2[d];
         h->cf32.inv[d] = (float)inv[d]; h->cf32.inv2[d] = (float)inv2[d];
     }
+    {   // the pair mode's tables: each FP64 coefficient as its nearest pair
+        CoefT<ff>& cp = h->cfp;
+        const CoefT<double>& cd = h->cf64;
+        for (int d = 0; d < 3; d++) {
+            for (int k = 0; k < 5; k++) {
+                cp.c1S[d][k] = ff(cd.c1S[d][k]); cp.c1V[d][k] = ff(cd.c1V[d][k]); cp.c2V[d][k] = ff(cd.c2V[d][k]);
+                cp.fq[d][k] = ff(cd.fq[d][k]); cp.fc[d][k] = ff(cd.fc[d][k]);
+            }
+            cp.inv[d] = ff(cd.inv[d]); cp.inv2[d] = ff(cd.inv2[d]);
+        }
+        cp.lam_mu = ff(cd.lam_mu);
+    }
 
     CK(cudaStreamCreateWithFlags(&h->own_stream, cudaStreamNonBlocking));
     h->stream = h->own_stream;
@@ -501,8 +546,8 @@ int cns_create(const cns_params* pin, int device, cns_solver** out) {
     for (int b = 0; b < 2; b++) {
         if (h->fp32)   // packed FP32 records (rho, u, v, w) and (T, p, H, mu)
             for (int f = 0; f < 2 && !rc; f++) rc = h->alloc_field(&h->der[b][f], sizeof(float4));
-        else
-            for (int f = 0; f < 4 && !rc; f++) rc = h->alloc_field(&h->der[b][f], rs);
+        else           // h, t, p, mu (pair mode: and rho, u, v, w)
+            for (int f = 0; f < (h->pair ? 8 : 4) && !rc; f++) rc = h->alloc_field(&h->der[b][f], rs);
     }
     if (!rc) rc = h->alloc_field(&h->dil, rs);
     if (!h->fp32)   // FP32-RHS: the RHS kernel forms the velocity gradients itself
@@ -519,6 +564,7 @@ int cns_create(const cns_params* pin, int device, cns_solver** out) {
     if (rc) { delete h; return rc; }
     h->cf64.xp = h->xp_d; h->cf64.cvsx = h->cvsx_d;
     h->cf32.xp = h->xp_f; h->cf32.cvsx = h->cvsx_f;
+    h->cfp.xp = h->xp_p; h->cfp.cvsx = h->cvsx_p;
     g.xp = h->xp_d; g.cvsx = h->cvsx_d; g.wvol = h->wvol_d; g.dxv = h->dxv_d;
 
     // zero every field once so ghost corners and unused padding hold finite values
@@ -735,6 +781,7 @@ int cns_calc_rhs(cns_solver* h, double* rr, double* ru, double* rv, double* rw, 
     const size_t N = (size_t)h->p.mx * h->p.my * h->p.mz;
     for (int f = 0; f < 5; f++) {
         if (h->fp32) launch_pack<float>(h->geom, (const float*)h->rb[f], h->staging, h->stream);
+        else if (h->pair) launch_pack<ff>(h->geom, (const ff*)h->rb[f], h->staging, h->stream);
         else launch_pack<double>(h->geom, (const double*)h->rb[f], h->staging, h->stream);
         h->launches++;
         if (out[f]) CK(cudaMemcpyAsync(out[f], h->staging, N * 8, cudaMemcpyDeviceToHost, h->stream));

@@ -26,7 +26,9 @@ struct cns_solver {
     Phys phys{};
     CoefT<double> cf64{};
     CoefT<float> cf32{};
+    CoefT<cns::ff> cfp{};        // pair mode
     bool fp32 = false;
+    bool pair = false;           // CNS_PREC_PAIR_RHS: RHS arithmetic in FP32 pairs (cns::ff)
     size_t rsz = 8;              // bytes of the RHS arithmetic type
     long long nalloc = 0;        // elements of one padded field
     std::vector<void*> allocs;
@@ -38,8 +40,9 @@ struct cns_solver {
     // stencil inputs derived from the state buffer q[b], in der[b]: FP64 mode h, t, p, mu
     // (the state itself gives rho, u, v, w); FP32-RHS mode der[b][0] = the packed records
     // (rho, u, v, w) and der[b][1] = (T, p, H, mu), float4 each. The RHS kernel reads those of
-    // q[cur] and writes those of the new state q[1 - cur] (fused state recovery)
-    void* der[2][4] = {};
+    // q[cur] and writes those of the new state q[1 - cur] (fused state recovery). Pair mode:
+    // der[b][0..3] = h, t, p, mu and der[b][4..7] = rho, u, v, w, all as pairs
+    void* der[2][8] = {};
     bool der_ok[2] = {false, false};   // der[b] holds the recovery of q[b]
     int mu_buf = 0;                    // buffer of the latest state recovery in program order of
                                        // the reference (its mu sets the CFL time step)
@@ -56,6 +59,7 @@ struct cns_solver {
     int diag_cap = 0;
     double *xp_d = nullptr, *cvsx_d = nullptr, *wvol_d = nullptr, *dxv_d = nullptr;
     float *xp_f = nullptr, *cvsx_f = nullptr;
+    cns::ff *xp_p = nullptr, *cvsx_p = nullptr;
     double *spx = nullptr, *spz = nullptr, *rref = nullptr, *uref = nullptr, *vref = nullptr, *wref = nullptr,
            *eref = nullptr;
     bool has_sponge = false;
@@ -132,7 +136,7 @@ inline void solver_set_parity(cns_solver* h, int want) {
         h->q[0][f] = h->q[1][f];
         h->q[1][f] = t;
     }
-    for (int f = 0; f < 4; f++) {
+    for (int f = 0; f < 8; f++) {
         void* a = h->der[0][f]; h->der[0][f] = h->der[1][f]; h->der[1][f] = a;
     }
     const bool ok0 = h->der_ok[0];

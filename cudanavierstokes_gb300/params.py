@@ -20,6 +20,7 @@ RK4_CLASSIC = 2
 
 PREC_FP64 = 0
 PREC_FP32_RHS = 1
+PREC_PAIR_RHS = 2   # RHS in FP32-pair (~48-bit) arithmetic, FP64 state
 
 # status codes (include/cns.h)
 CNS_OK = 0

@@ -67,6 +67,9 @@ extern "C" {
 #define CNS_PREC_FP64      0   /* plain FP64 everywhere, as the reference                */
 #define CNS_PREC_FP32_RHS  1   /* RHS in FP32; state, RK accumulation, T/p recovery and
                                   reductions in FP64                                     */
+#define CNS_PREC_PAIR_RHS  2   /* RHS in FP32-pair ("double-float", ~48-bit) arithmetic;
+                                  state, RK accumulation, T/p recovery and reductions
+                                  in FP64 (single solvers; batches take modes 0 and 1)   */
 
 /*
  * Runtime mirror of the reference's compile-time parameter surface
@@ -94,7 +97,7 @@ typedef struct cns_params {
     int32_t check_bulk;          /* checkBulk: bulk / kinetic-energy diagnostic period    */
     int32_t quirk_dissipation_y; /* 1: reproduce the reference's y viscous-dissipation
                                     term tau_yz*dv/dz (src/cuda_rhs.cu:175); 0: tau_yz*dw/dy */
-    int32_t precision;           /* CNS_PREC_FP64 or CNS_PREC_FP32_RHS                     */
+    int32_t precision;           /* CNS_PREC_FP64, CNS_PREC_FP32_RHS or CNS_PREC_PAIR_RHS  */
     int32_t ndivz;               /* nDivZ (globals.h:58): accepted for compatibility, no effect */
     double  dpdz_init;           /* initial body force when forcing (cuda_utils.cu:69: 0.00372) */
     /* sponge constants (src/sponge.h:4-17) */
