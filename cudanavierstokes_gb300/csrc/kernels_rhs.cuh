@@ -73,19 +73,28 @@ __device__ __forceinline__ R d2x_nu(const Get& get, const R* __restrict__ cvsx, 
     return s;
 }
 
+// f(a[k]) for k = 0, 1, 2 of a register array, with k a literal after inlining or uniform
+// at run time: branches, no indexed (local-memory) access
+template <typename T, int N, class F>
+__device__ __forceinline__ void at3(T (&a)[N], int k, F f) {
+    if (k == 0) f(a[0]); else if (k == 1) f(a[1]); else f(a[2]);
+}
+
 // FP64 body: contribution of direction DIR (deviceRHSX/Y/Z) on the separate stencil fields.
 // Terms that every direction multiplies by the same centre value are summed over the
 // directions first and multiplied once per point (rhs_point_nb): the second derivatives of
 // u, v, w, T in L[] (times mu), the viscous momentum terms grad mu . s + mu/3 grad theta in
 // W[] (the energy equation's work u_i W_i), the conduction in cond (times lambda/mu), and
 // the mass flux, whose half carries the centre value of the four cubic fluxes. The stress
-// row tau_{DIR,c}/mu comes from rhs_point_nb, which forms the symmetric tensor once.
+// row tau_{DIR,c}/mu comes from rhs_point_nb, which forms the symmetric tensor once. The
+// direction is an argument: called with a literal it folds like a template parameter; the
+// pair type calls it in a loop that is not unrolled (rhs_point_nb).
 // (The FP32-RHS mode has its own body on the packed records, rhs_dir_packed below.)
-template <typename R, int S, int V, int DIR, class NB>
-__device__ __forceinline__ void rhs_direction(const Geom& g, const CoefT<R>& cf, const NB& nb, int i,
+template <typename R, int S, int V, bool MAYBE_X, class NB>
+__device__ __forceinline__ void rhs_direction(const Geom& g, const CoefT<R>& cf, const NB& nb, int i, const int DIR,
                                               const R (&tau)[3], R m3, R u0, R v0, R w0, R r0, R (&acc)[5],
                                               R (&W)[3], R (&L)[4], R& cond) {
-    const bool nux = (DIR == 0) && g.nonuniform_x;
+    const bool nux = MAYBE_X && DIR == 0 && g.nonuniform_x;   // MAYBE_X false: y or z (folds)
     const R xpi = nux ? cf.xp[i] : (R)1;
     const R* c1V = cf.c1V[DIR];
     const R* c1S = cf.c1S[DIR];
@@ -138,7 +147,7 @@ __device__ __forceinline__ void rhs_direction(const Geom& g, const CoefT<R>& cf,
     // mu/3 d(theta) on the DIR momentum (and its work), pressure gradient
     const R dth = d1<R, V>(gd, c1V) * xpi;
     const R dp = d1<R, S>(gp, c1S) * xpi;
-    W[DIR] = fma(m3, dth, W[DIR]);
+    at3(W, MAYBE_X ? DIR : (DIR == 1 ? 1 : 2), [&](R& w) { w = fma(m3, dth, w); });
 
     // split-form convective derivatives, telescoped (see file comment); with a uniform
     // spacing the flux weights already carry 1/2 or 1/4 and 1/dx, so they accumulate
@@ -152,7 +161,7 @@ __device__ __forceinline__ void rhs_direction(const Geom& g, const CoefT<R>& cf,
     // The mass flux weights are twice the cubic ones (fq = 0.5 c1S, fc = 0.25 c1S: exactly
     // 2 fc), so the mass flux is 2 sum_l (a_l Q- - a_l Q+); a_l Q+- = (a_l rho_0 + a_l rho_+-)
     // (g_+- + g_0) with a_l rho_0 shared by the two: 17 operations per l.
-    const R un = DIR == 0 ? u0 : (DIR == 1 ? v0 : w0);
+    const R un = (MAYBE_X && DIR == 0) ? u0 : (DIR == 1 ? v0 : w0);
     R sd = (R)0, fu = nux ? (R)0 : acc[1], fv = nux ? (R)0 : acc[2], fw = nux ? (R)0 : acc[3],
       fe = nux ? (R)0 : acc[4];
     const R* fcb = cf.fc[DIR];
@@ -163,8 +172,8 @@ __device__ __forceinline__ void rhs_direction(const Geom& g, const CoefT<R>& cf,
         const R vm = vs[S - l], vp = vs[S + l];
         const R wm = ws[S - l], wp = ws[S + l];
         const R hm = nb.h(-l), hp = nb.h(l);
-        const R gm = DIR == 0 ? um : (DIR == 1 ? vm : wm);
-        const R gp = DIR == 0 ? up : (DIR == 1 ? vp : wp);
+        const R gm = (MAYBE_X && DIR == 0) ? um : (DIR == 1 ? vm : wm);
+        const R gp = (MAYBE_X && DIR == 0) ? up : (DIR == 1 ? vp : wp);
         const R ar0 = fcb[l] * r0;
         const R am = fma(fcb[l], rm, ar0) * (gm + un);
         const R ap = fma(fcb[l], rp, ar0) * (un + gp);
@@ -184,7 +193,7 @@ __device__ __forceinline__ void rhs_direction(const Geom& g, const CoefT<R>& cf,
     } else {
         acc[0] = fr; acc[1] = fu; acc[2] = fv; acc[3] = fw; acc[4] = fe;
     }
-    acc[1 + DIR] -= dp;
+    if (MAYBE_X && DIR == 0) acc[1] -= dp; else if (DIR == 1) acc[2] -= dp; else acc[3] -= dp;
 }
 
 // Body force, sponge, stage update and the new state's recovery of the point at element
@@ -319,9 +328,24 @@ __device__ __forceinline__ void rhs_point_nb(const Geom& g, const CoefT<R>& cf, 
     R W[3] = {0, 0, 0};
     R L[4] = {0, 0, 0, 0};
     R cond = 0;
-    rhs_direction<R, S, V, 0>(g, cf, nx, i, tx, m3, u0, v0, w0, r0, acc, W, L, cond);
-    rhs_direction<R, S, V, 1>(g, cf, ny, i, ty, m3, u0, v0, w0, r0, acc, W, L, cond);
-    rhs_direction<R, S, V, 2>(g, cf, nz, i, tz, m3, u0, v0, w0, r0, acc, W, L, cond);
+    if constexpr (is_ff<R> && std::is_same<NX, NbGlobal<R>>::value && std::is_same<NY, NX>::value &&
+                  std::is_same<NZ, NX>::value) {
+        // the pair arithmetic is ~15 instructions per operation: x (with the stretched-grid
+        // terms) and one copy of the y / z body walked twice keep the kernel's code within
+        // the instruction caches
+        rhs_direction<R, S, V, true>(g, cf, nx, i, 0, tx, m3, u0, v0, w0, r0, acc, W, L, cond);
+#pragma unroll 1
+        for (int d = 1; d < 3; d++) {
+            const R td[3] = {d == 1 ? t01 : t02, d == 1 ? t11 : t12, d == 1 ? t12 : t22};
+            NX nb = ny;   // the accessors differ in their stride only
+            nb.st = d == 1 ? ny.st : nz.st;
+            rhs_direction<R, S, V, false>(g, cf, nb, i, d, td, m3, u0, v0, w0, r0, acc, W, L, cond);
+        }
+    } else {
+        rhs_direction<R, S, V, true>(g, cf, nx, i, 0, tx, m3, u0, v0, w0, r0, acc, W, L, cond);
+        rhs_direction<R, S, V, false>(g, cf, ny, i, 1, ty, m3, u0, v0, w0, r0, acc, W, L, cond);
+        rhs_direction<R, S, V, false>(g, cf, nz, i, 2, tz, m3, u0, v0, w0, r0, acc, W, L, cond);
+    }
     // the centre values of the cubic fluxes: phi_0 times half the mass flux
     const R half = (R)0.5 * acc[0];
     acc[1] = fma(u0, half, acc[1]);
@@ -535,7 +559,8 @@ __device__ __forceinline__ void rhs_point(const Geom& g, const CoefT<R>& cf, con
 
 // FP32: 7 blocks of 128 per SM (72 registers) measured fastest (6: 80 registers, +13 %
 // time; 5: 96 registers, and stages that read the RK register ran 3.5x slower); FP64: the
-// FP64 pipe bounds the kernel at 3 to 5 blocks alike
+// FP64 pipe bounds the kernel at 3 to 5 blocks alike; pairs: 4 blocks (128 registers, 60 B
+// of spills) 703 Mpoint-steps/s on the channel against 686 with 3 blocks (168, none)
 //
 // One launch covers the 4-row bands [band0, band0 + gridDim.y) of every plane; blocks are
 // dispatched x fastest, then bands, then planes. On large planes the bands are split into
@@ -543,7 +568,8 @@ __device__ __forceinline__ void rhs_point(const Geom& g, const CoefT<R>& cf, con
 // group's blocks sweep them (one launch over whole planes would cycle ~2S planes of the
 // inputs through L2 between their uses).
 template <typename R, int S, int V>
-__global__ void __launch_bounds__(128, sizeof(R) == 4 ? 7 : 4) k_rhs(Geom g, CoefT<R> cf, RhsIn<R> in, Update<R> up,
+__global__ void __launch_bounds__(128, sizeof(R) == 4 ? 7 : 4) k_rhs(Geom g, const __grid_constant__ CoefT<R> cf,
+                                                                                   const __grid_constant__ RhsIn<R> in, Update<R> up,
                                              double* __restrict__ scal, int quirk, int band0) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     const int j = (band0 + (int)blockIdx.y) * blockDim.y + threadIdx.y;
