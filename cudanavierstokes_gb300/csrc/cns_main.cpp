@@ -7,7 +7,7 @@
 // (mx_tot, my_tot, mz_tot, Lx, Ly, Lz, stencilSize, stencilVisc, nsteps, nfiles, CFL,
 // restartFile, lowStorage, boundaryLayer, perturbed, forcing, periodicX, nonUniformX,
 // checkCFLcondition, checkBulk, Re, Pr, Ma, viscexp, gam, stretch, TwallTop, TwallBot) plus
-// optional precision (0 FP64, 1 FP32 RHS) and quirk_dissipation_y. Output as the reference:
+// optional precision (0 FP64, 1 FP32 RHS, 2 FP32-pair RHS) and quirk_dissipation_y. Output as the reference:
 // fields/{x,y,z}.bin, Grid.txt, fields/{r,u,v,w,e}.%07d.bin (raw FP64, [k][j][i]),
 // solution.txt ("step time kin par2 dtime" every checkCFLcondition steps), prof.txt (plane
 // profiles, after each file) and the printed friction Reynolds number, and an XDMF
