@@ -196,6 +196,89 @@ __device__ __forceinline__ void rhs_direction(const Geom& g, const CoefT<R>& cf,
     if (MAYBE_X && DIR == 0) acc[1] -= dp; else if (DIR == 1) acc[2] -= dp; else acc[3] -= dp;
 }
 
+// Pair-type body of one direction: the sums of rhs_direction in one pass over the offsets
+// l = 1..S that is not unrolled (the pair arithmetic is ~15 instructions per operation, and
+// the unrolled body does not fit the instruction caches). At each l it loads the neighbours
+// on either side and feeds every sum that needs them; each sum keeps rhs_direction's order
+// (centre term, then l ascending), except the stretched-x second derivative, which adds the
+// pair (-l, l) per l.
+template <int S, int V, bool MAYBE_X>
+__device__ __forceinline__ void rhs_dir_pair(const Geom& g, const CoefT<ff>& cf, const NbGlobal<ff>& nb, int i,
+                                             const int DIR, const ff (&tau)[3], ff m3, ff u0, ff v0, ff w0, ff r0,
+                                             ff (&acc)[5], ff (&W)[3], ff (&L)[4], ff& cond) {
+    const bool nux = MAYBE_X && DIR == 0 && g.nonuniform_x;
+    const ff t0 = nb.t(0);
+    if (nux) {
+        const ff cw = __ldg(cf.cvsx + V * g.mx + i);
+        L[0] = fma(cw, u0, L[0]); L[1] = fma(cw, v0, L[1]); L[2] = fma(cw, w0, L[2]); L[3] = fma(cw, t0, L[3]);
+    } else {
+        const ff cw = cf.c2V[DIR][0];
+        L[0] = fma(cw, u0, L[0]); L[1] = fma(cw, v0, L[1]); L[2] = fma(cw, w0, L[2]); L[3] = fma(cw, t0, L[3]);
+    }
+    const ff un = (MAYBE_X && DIR == 0) ? u0 : (DIR == 1 ? v0 : w0);
+    ff dmu(0), dt(0), dth(0), dp(0), sd(0);
+    ff fu = nux ? ff(0) : acc[1], fv = nux ? ff(0) : acc[2], fw = nux ? ff(0) : acc[3], fe = nux ? ff(0) : acc[4];
+#pragma unroll 1
+    for (int l = 1; l <= S; l++) {
+        const ff um = nb.u(-l), up = nb.u(l), vm = nb.v(-l), vp = nb.v(l), wm = nb.w(-l), wp = nb.w(l);
+        dp = fma(cf.c1S[DIR][l], nb.p(l) - nb.p(-l), dp);
+        if (l <= V) {
+            const ff c1 = cf.c1V[DIR][l];
+            dmu = fma(c1, nb.m(l) - nb.m(-l), dmu);
+            const ff tm = nb.t(-l), tp = nb.t(l);
+            dt = fma(c1, tp - tm, dt);
+            dth = fma(c1, nb.dil(l) - nb.dil(-l), dth);
+            if (nux) {
+                const ff cm = __ldg(cf.cvsx + (V - l) * g.mx + i), cp = __ldg(cf.cvsx + (V + l) * g.mx + i);
+                L[0] = fma(cp, up, fma(cm, um, L[0]));
+                L[1] = fma(cp, vp, fma(cm, vm, L[1]));
+                L[2] = fma(cp, wp, fma(cm, wm, L[2]));
+                L[3] = fma(cp, tp, fma(cm, tm, L[3]));
+            } else {
+                const ff c2 = cf.c2V[DIR][l];
+                L[0] = fma(c2, up + um, L[0]);
+                L[1] = fma(c2, vp + vm, L[1]);
+                L[2] = fma(c2, wp + wm, L[2]);
+                L[3] = fma(c2, tp + tm, L[3]);
+            }
+        }
+        // telescoped split-form fluxes (rhs_direction)
+        const ff rm = nb.r(-l), rp = nb.r(l), hm = nb.h(-l), hp = nb.h(l);
+        const ff gm = (MAYBE_X && DIR == 0) ? um : (DIR == 1 ? vm : wm);
+        const ff gp = (MAYBE_X && DIR == 0) ? up : (DIR == 1 ? vp : wp);
+        const ff fc = cf.fc[DIR][l];
+        const ff ar0 = fc * r0;
+        const ff am = fma(fc, rm, ar0) * (gm + un);
+        const ff ap = fma(fc, rp, ar0) * (un + gp);
+        sd += am - ap;
+        fu = fma(am, um, fma(-ap, up, fu));
+        fv = fma(am, vm, fma(-ap, vp, fv));
+        fw = fma(am, wm, fma(-ap, wp, fw));
+        fe = fma(am, hm, fma(-ap, hp, fe));
+    }
+    if (nux) {
+        const ff xpi = cf.xp[i];
+        dmu *= xpi; dt *= xpi; dth *= xpi; dp *= xpi;
+    }
+    W[0] = fma(tau[0], dmu, W[0]);
+    W[1] = fma(tau[1], dmu, W[1]);
+    W[2] = fma(tau[2], dmu, W[2]);
+    cond = fma(dt, dmu, cond);
+    at3(W, MAYBE_X ? DIR : (DIR == 1 ? 1 : 2), [&](ff& w) { w = fma(m3, dth, w); });
+    const ff fr = nux ? sd + sd : fma(ff(2), sd, acc[0]);
+    if (nux) {
+        const ff xpi = cf.xp[i];
+        acc[0] = fma(xpi, fr, acc[0]);
+        acc[1] = fma(xpi, fu, acc[1]);
+        acc[2] = fma(xpi, fv, acc[2]);
+        acc[3] = fma(xpi, fw, acc[3]);
+        acc[4] = fma(xpi, fe, acc[4]);
+    } else {
+        acc[0] = fr; acc[1] = fu; acc[2] = fv; acc[3] = fw; acc[4] = fe;
+    }
+    if (MAYBE_X && DIR == 0) acc[1] -= dp; else if (DIR == 1) acc[2] -= dp; else acc[3] -= dp;
+}
+
 // Body force, sponge, stage update and the new state's recovery of the point at element
 // c, given its RHS accumulators acc (convective, pressure and viscous terms) and centre
 // values u0, v0, w0, r0 in the arithmetic type R
@@ -331,15 +414,15 @@ __device__ __forceinline__ void rhs_point_nb(const Geom& g, const CoefT<R>& cf, 
     if constexpr (is_ff<R> && std::is_same<NX, NbGlobal<R>>::value && std::is_same<NY, NX>::value &&
                   std::is_same<NZ, NX>::value) {
         // the pair arithmetic is ~15 instructions per operation: x (with the stretched-grid
-        // terms) and one copy of the y / z body walked twice keep the kernel's code within
-        // the instruction caches
-        rhs_direction<R, S, V, true>(g, cf, nx, i, 0, tx, m3, u0, v0, w0, r0, acc, W, L, cond);
+        // terms) and one copy of the y / z body walked twice, each a loop over the offsets
+        // (rhs_dir_pair), keep the kernel's code within the instruction caches
+        rhs_dir_pair<S, V, true>(g, cf, nx, i, 0, tx, m3, u0, v0, w0, r0, acc, W, L, cond);
 #pragma unroll 1
         for (int d = 1; d < 3; d++) {
             const R td[3] = {d == 1 ? t01 : t02, d == 1 ? t11 : t12, d == 1 ? t12 : t22};
             NX nb = ny;   // the accessors differ in their stride only
             nb.st = d == 1 ? ny.st : nz.st;
-            rhs_direction<R, S, V, false>(g, cf, nb, i, d, td, m3, u0, v0, w0, r0, acc, W, L, cond);
+            rhs_dir_pair<S, V, false>(g, cf, nb, i, d, td, m3, u0, v0, w0, r0, acc, W, L, cond);
         }
     } else {
         rhs_direction<R, S, V, true>(g, cf, nx, i, 0, tx, m3, u0, v0, w0, r0, acc, W, L, cond);
@@ -559,8 +642,8 @@ __device__ __forceinline__ void rhs_point(const Geom& g, const CoefT<R>& cf, con
 
 // FP32: 7 blocks of 128 per SM (72 registers) measured fastest (6: 80 registers, +13 %
 // time; 5: 96 registers, and stages that read the RK register ran 3.5x slower); FP64: the
-// FP64 pipe bounds the kernel at 3 to 5 blocks alike; pairs: 4 blocks (128 registers, 60 B
-// of spills) 703 Mpoint-steps/s on the channel against 686 with 3 blocks (168, none)
+// FP64 pipe bounds the kernel at 3 to 5 blocks alike; pairs: 4 blocks (122 registers)
+// 856 Mpoint-steps/s on the channel against 815 with 5 (96 registers)
 //
 // One launch covers the 4-row bands [band0, band0 + gridDim.y) of every plane; blocks are
 // dispatched x fastest, then bands, then planes. On large planes the bands are split into
