@@ -216,30 +216,32 @@ __device__ __forceinline__ void rhs_dir_pair(const Geom& g, const CoefT<ff>& cf,
         L[0] = fma(cw, u0, L[0]); L[1] = fma(cw, v0, L[1]); L[2] = fma(cw, w0, L[2]); L[3] = fma(cw, t0, L[3]);
     }
     const ff un = (MAYBE_X && DIR == 0) ? u0 : (DIR == 1 ? v0 : w0);
-    ff dmu(0), dt(0), dth(0), dp(0), sd(0);
-    ff fu = nux ? ff(0) : acc[1], fv = nux ? ff(0) : acc[2], fw = nux ? ff(0) : acc[3], fe = nux ? ff(0) : acc[4];
+    const ff zero(0);
+    ffacc Dmu(zero), Dt(zero), Dth(zero), Dp(zero), Sd(zero);
+    ffacc La[4] = {ffacc(L[0]), ffacc(L[1]), ffacc(L[2]), ffacc(L[3])};
+    ffacc Fu(nux ? zero : acc[1]), Fv(nux ? zero : acc[2]), Fw(nux ? zero : acc[3]), Fe(nux ? zero : acc[4]);
 #pragma unroll 1
     for (int l = 1; l <= S; l++) {
         const ff um = nb.u(-l), up = nb.u(l), vm = nb.v(-l), vp = nb.v(l), wm = nb.w(-l), wp = nb.w(l);
-        dp = fma(cf.c1S[DIR][l], nb.p(l) - nb.p(-l), dp);
+        Dp.add_prod(cf.c1S[DIR][l], nb.p(l) - nb.p(-l));
         if (l <= V) {
             const ff c1 = cf.c1V[DIR][l];
-            dmu = fma(c1, nb.m(l) - nb.m(-l), dmu);
+            Dmu.add_prod(c1, nb.m(l) - nb.m(-l));
             const ff tm = nb.t(-l), tp = nb.t(l);
-            dt = fma(c1, tp - tm, dt);
-            dth = fma(c1, nb.dil(l) - nb.dil(-l), dth);
+            Dt.add_prod(c1, tp - tm);
+            Dth.add_prod(c1, nb.dil(l) - nb.dil(-l));
             if (nux) {
                 const ff cm = __ldg(cf.cvsx + (V - l) * g.mx + i), cp = __ldg(cf.cvsx + (V + l) * g.mx + i);
-                L[0] = fma(cp, up, fma(cm, um, L[0]));
-                L[1] = fma(cp, vp, fma(cm, vm, L[1]));
-                L[2] = fma(cp, wp, fma(cm, wm, L[2]));
-                L[3] = fma(cp, tp, fma(cm, tm, L[3]));
+                La[0].add_prod(cm, um); La[0].add_prod(cp, up);
+                La[1].add_prod(cm, vm); La[1].add_prod(cp, vp);
+                La[2].add_prod(cm, wm); La[2].add_prod(cp, wp);
+                La[3].add_prod(cm, tm); La[3].add_prod(cp, tp);
             } else {
                 const ff c2 = cf.c2V[DIR][l];
-                L[0] = fma(c2, up + um, L[0]);
-                L[1] = fma(c2, vp + vm, L[1]);
-                L[2] = fma(c2, wp + wm, L[2]);
-                L[3] = fma(c2, tp + tm, L[3]);
+                La[0].add_prod(c2, up + um);
+                La[1].add_prod(c2, vp + vm);
+                La[2].add_prod(c2, wp + wm);
+                La[3].add_prod(c2, tp + tm);
             }
         }
         // telescoped split-form fluxes (rhs_direction)
@@ -249,13 +251,16 @@ __device__ __forceinline__ void rhs_dir_pair(const Geom& g, const CoefT<ff>& cf,
         const ff fc = cf.fc[DIR][l];
         const ff ar0 = fc * r0;
         const ff am = fma(fc, rm, ar0) * (gm + un);
-        const ff ap = fma(fc, rp, ar0) * (un + gp);
-        sd += am - ap;
-        fu = fma(am, um, fma(-ap, up, fu));
-        fv = fma(am, vm, fma(-ap, vp, fv));
-        fw = fma(am, wm, fma(-ap, wp, fw));
-        fe = fma(am, hm, fma(-ap, hp, fe));
+        const ff ap = -(fma(fc, rp, ar0) * (un + gp));
+        Sd.add(am); Sd.add(ap);
+        Fu.add_prod(am, um); Fu.add_prod(ap, up);
+        Fv.add_prod(am, vm); Fv.add_prod(ap, vp);
+        Fw.add_prod(am, wm); Fw.add_prod(ap, wp);
+        Fe.add_prod(am, hm); Fe.add_prod(ap, hp);
     }
+    for (int q = 0; q < 4; q++) L[q] = La[q].value();
+    ff dmu = Dmu.value(), dt = Dt.value(), dth = Dth.value(), dp = Dp.value();
+    const ff sd = Sd.value(), fu = Fu.value(), fv = Fv.value(), fw = Fw.value(), fe = Fe.value();
     if (nux) {
         const ff xpi = cf.xp[i];
         dmu *= xpi; dt *= xpi; dth *= xpi; dp *= xpi;
