@@ -107,6 +107,83 @@ struct ffacc {
     __device__ __forceinline__ ff value() const { return two_sum(h, l); }
 };
 
+// Two pairs side by side (lane x, lane y) through Blackwell's packed FP32x2 instructions
+// (__fadd2_rn, __fmul2_rn, __ffma2_rn): the same algorithms as above, two independent pair
+// operations per instruction sequence.
+struct ff2 {
+    float2 h, l;
+};
+
+__device__ __forceinline__ ff2 mk2(ff a, ff b) { return ff2{make_float2(a.h, b.h), make_float2(a.l, b.l)}; }
+__device__ __forceinline__ ff lane0(ff2 v) { return ff(v.h.x, v.l.x); }
+__device__ __forceinline__ ff lane1(ff2 v) { return ff(v.h.y, v.l.y); }
+
+__device__ __forceinline__ float2 neg2(float2 a) { return make_float2(-a.x, -a.y); }
+__device__ __forceinline__ float2 add2(float2 a, float2 b) { return __fadd2_rn(a, b); }
+__device__ __forceinline__ float2 sub2(float2 a, float2 b) { return __fadd2_rn(a, neg2(b)); }
+
+__device__ __forceinline__ void fast_two_sum2(float2 a, float2 b, float2& s, float2& e) {
+    s = add2(a, b);
+    e = sub2(b, sub2(s, a));
+}
+__device__ __forceinline__ void two_sum2(float2 a, float2 b, float2& s, float2& e) {
+    s = add2(a, b);
+    const float2 bb = sub2(s, a);
+    e = add2(sub2(a, sub2(s, bb)), sub2(b, bb));
+}
+
+__device__ __forceinline__ ff2 operator+(ff2 x, ff2 y) {
+    float2 sh, sl, zh, zl;
+    two_sum2(x.h, y.h, sh, sl);
+    fast_two_sum2(sh, add2(sl, add2(x.l, y.l)), zh, zl);
+    return ff2{zh, zl};
+}
+__device__ __forceinline__ ff2 operator-(ff2 x) { return ff2{neg2(x.h), neg2(x.l)}; }
+__device__ __forceinline__ ff2 operator-(ff2 x, ff2 y) { return x + (-y); }
+
+__device__ __forceinline__ void mul_parts2(ff2 x, ff2 y, float2& ch, float2& cl) {
+    ch = __fmul2_rn(x.h, y.h);
+    const float2 cl1 = __ffma2_rn(x.h, y.h, neg2(ch));
+    cl = add2(cl1, __ffma2_rn(x.l, y.h, __fmul2_rn(x.h, y.l)));
+}
+__device__ __forceinline__ ff2 operator*(ff2 x, ff2 y) {
+    float2 ch, cl, zh, zl;
+    mul_parts2(x, y, ch, cl);
+    fast_two_sum2(ch, cl, zh, zl);
+    return ff2{zh, zl};
+}
+__device__ __forceinline__ ff2 fma(ff2 a, ff2 b, ff2 c) {
+    float2 ph, pl, sh, sl, zh, zl;
+    mul_parts2(a, b, ph, pl);
+    two_sum2(ph, c.h, sh, sl);
+    fast_two_sum2(sh, add2(sl, add2(pl, c.l)), zh, zl);
+    return ff2{zh, zl};
+}
+
+// ffacc on two lanes
+struct ffacc2 {
+    float2 h, l;
+    __device__ __forceinline__ explicit ffacc2(ff2 x) : h(x.h), l(x.l) {}
+    __device__ __forceinline__ void add_prod(ff2 a, ff2 b) {
+        float2 ph, pl, sh, sl;
+        mul_parts2(a, b, ph, pl);
+        two_sum2(h, ph, sh, sl);
+        h = sh;
+        l = add2(l, add2(sl, pl));
+    }
+    __device__ __forceinline__ void add(ff2 a) {
+        float2 sh, sl;
+        two_sum2(h, a.h, sh, sl);
+        h = sh;
+        l = add2(l, add2(sl, a.l));
+    }
+    __device__ __forceinline__ ff2 value() const {
+        float2 zh, zl;
+        two_sum2(h, l, zh, zl);
+        return ff2{zh, zl};
+    }
+};
+
 template <typename R>
 inline constexpr bool is_ff = false;
 template <>

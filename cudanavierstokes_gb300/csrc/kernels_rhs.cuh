@@ -217,50 +217,50 @@ __device__ __forceinline__ void rhs_dir_pair(const Geom& g, const CoefT<ff>& cf,
     }
     const ff un = (MAYBE_X && DIR == 0) ? u0 : (DIR == 1 ? v0 : w0);
     const ff zero(0);
-    ffacc Dmu(zero), Dt(zero), Dth(zero), Dp(zero), Sd(zero);
-    ffacc La[4] = {ffacc(L[0]), ffacc(L[1]), ffacc(L[2]), ffacc(L[3])};
-    ffacc Fu(nux ? zero : acc[1]), Fv(nux ? zero : acc[2]), Fw(nux ? zero : acc[3]), Fe(nux ? zero : acc[4]);
+    const ff2 zero2 = mk2(zero, zero), un2 = mk2(un, un);
+    // lanes: (p, theta), (mu, T), (L_u, L_v), (L_w, L_T), (F_u, F_v), (F_w, F_e), and the mass
+    // flux as (sum a_l Q-, -sum a_l Q+)
+    ffacc2 Dpth(zero2), Dmt(zero2), Luv(mk2(L[0], L[1])), Lwt(mk2(L[2], L[3])), Sd(zero2);
+    ffacc2 Fuv(nux ? zero2 : mk2(acc[1], acc[2])), Fwe(nux ? zero2 : mk2(acc[3], acc[4]));
 #pragma unroll 1
     for (int l = 1; l <= S; l++) {
         const ff um = nb.u(-l), up = nb.u(l), vm = nb.v(-l), vp = nb.v(l), wm = nb.w(-l), wp = nb.w(l);
-        Dp.add_prod(cf.c1S[DIR][l], nb.p(l) - nb.p(-l));
+        // theta's weight is zero beyond the viscous half-width (its ghosts hold finite values)
+        Dpth.add_prod(mk2(cf.c1S[DIR][l], l <= V ? cf.c1V[DIR][l] : zero),
+                      mk2(nb.p(l), nb.dil(l)) - mk2(nb.p(-l), nb.dil(-l)));
         if (l <= V) {
             const ff c1 = cf.c1V[DIR][l];
-            Dmu.add_prod(c1, nb.m(l) - nb.m(-l));
             const ff tm = nb.t(-l), tp = nb.t(l);
-            Dt.add_prod(c1, tp - tm);
-            Dth.add_prod(c1, nb.dil(l) - nb.dil(-l));
+            Dmt.add_prod(mk2(c1, c1), mk2(nb.m(l), tp) - mk2(nb.m(-l), tm));
             if (nux) {
                 const ff cm = __ldg(cf.cvsx + (V - l) * g.mx + i), cp = __ldg(cf.cvsx + (V + l) * g.mx + i);
-                La[0].add_prod(cm, um); La[0].add_prod(cp, up);
-                La[1].add_prod(cm, vm); La[1].add_prod(cp, vp);
-                La[2].add_prod(cm, wm); La[2].add_prod(cp, wp);
-                La[3].add_prod(cm, tm); La[3].add_prod(cp, tp);
+                const ff2 cm2 = mk2(cm, cm), cp2 = mk2(cp, cp);
+                Luv.add_prod(cm2, mk2(um, vm)); Luv.add_prod(cp2, mk2(up, vp));
+                Lwt.add_prod(cm2, mk2(wm, tm)); Lwt.add_prod(cp2, mk2(wp, tp));
             } else {
                 const ff c2 = cf.c2V[DIR][l];
-                La[0].add_prod(c2, up + um);
-                La[1].add_prod(c2, vp + vm);
-                La[2].add_prod(c2, wp + wm);
-                La[3].add_prod(c2, tp + tm);
+                const ff2 c22 = mk2(c2, c2);
+                Luv.add_prod(c22, mk2(up, vp) + mk2(um, vm));
+                Lwt.add_prod(c22, mk2(wp, tp) + mk2(wm, tm));
             }
         }
-        // telescoped split-form fluxes (rhs_direction)
-        const ff rm = nb.r(-l), rp = nb.r(l), hm = nb.h(-l), hp = nb.h(l);
+        // telescoped split-form fluxes (rhs_direction): lanes (a_l Q-, a_l Q+)
         const ff gm = (MAYBE_X && DIR == 0) ? um : (DIR == 1 ? vm : wm);
         const ff gp = (MAYBE_X && DIR == 0) ? up : (DIR == 1 ? vp : wp);
         const ff fc = cf.fc[DIR][l];
         const ff ar0 = fc * r0;
-        const ff am = fma(fc, rm, ar0) * (gm + un);
-        const ff ap = -(fma(fc, rp, ar0) * (un + gp));
-        Sd.add(am); Sd.add(ap);
-        Fu.add_prod(am, um); Fu.add_prod(ap, up);
-        Fv.add_prod(am, vm); Fv.add_prod(ap, vp);
-        Fw.add_prod(am, wm); Fw.add_prod(ap, wp);
-        Fe.add_prod(am, hm); Fe.add_prod(ap, hp);
+        const ff2 q = fma(mk2(fc, fc), mk2(nb.r(-l), nb.r(l)), mk2(ar0, ar0)) * (mk2(gm, gp) + un2);
+        const ff2 qs = ff2{make_float2(q.h.x, -q.h.y), make_float2(q.l.x, -q.l.y)};   // (a_l Q-, -a_l Q+)
+        Sd.add(qs);
+        const ff2 am2 = mk2(lane0(qs), lane0(qs)), ap2 = mk2(lane1(qs), lane1(qs));
+        Fuv.add_prod(am2, mk2(um, vm)); Fuv.add_prod(ap2, mk2(up, vp));
+        Fwe.add_prod(am2, mk2(wm, nb.h(-l))); Fwe.add_prod(ap2, mk2(wp, nb.h(l)));
     }
-    for (int q = 0; q < 4; q++) L[q] = La[q].value();
-    ff dmu = Dmu.value(), dt = Dt.value(), dth = Dth.value(), dp = Dp.value();
-    const ff sd = Sd.value(), fu = Fu.value(), fv = Fv.value(), fw = Fw.value(), fe = Fe.value();
+    const ff2 luv = Luv.value(), lwt = Lwt.value(), pth = Dpth.value(), mt = Dmt.value();
+    const ff2 s2 = Sd.value(), fuv = Fuv.value(), fwe = Fwe.value();
+    L[0] = lane0(luv); L[1] = lane1(luv); L[2] = lane0(lwt); L[3] = lane1(lwt);
+    ff dmu = lane0(mt), dt = lane1(mt), dth = lane1(pth), dp = lane0(pth);
+    const ff sd = lane0(s2) + lane1(s2), fu = lane0(fuv), fv = lane1(fuv), fw = lane0(fwe), fe = lane1(fwe);
     if (nux) {
         const ff xpi = cf.xp[i];
         dmu *= xpi; dt *= xpi; dth *= xpi; dp *= xpi;
