@@ -118,9 +118,11 @@ __device__ __forceinline__ ff2 mk2(ff a, ff b) { return ff2{make_float2(a.h, b.h
 __device__ __forceinline__ ff lane0(ff2 v) { return ff(v.h.x, v.l.x); }
 __device__ __forceinline__ ff lane1(ff2 v) { return ff(v.h.y, v.l.y); }
 
-__device__ __forceinline__ float2 neg2(float2 a) { return make_float2(-a.x, -a.y); }
+// negation and subtraction as one packed instruction each: b (-1) + a rounds once, exactly
+// like a - b; a (-1) is exact
+__device__ __forceinline__ float2 neg2(float2 a) { return __fmul2_rn(a, make_float2(-1.0f, -1.0f)); }
 __device__ __forceinline__ float2 add2(float2 a, float2 b) { return __fadd2_rn(a, b); }
-__device__ __forceinline__ float2 sub2(float2 a, float2 b) { return __fadd2_rn(a, neg2(b)); }
+__device__ __forceinline__ float2 sub2(float2 a, float2 b) { return __ffma2_rn(b, make_float2(-1.0f, -1.0f), a); }
 
 __device__ __forceinline__ void fast_two_sum2(float2 a, float2 b, float2& s, float2& e) {
     s = add2(a, b);

@@ -250,7 +250,8 @@ __device__ __forceinline__ void rhs_dir_pair(const Geom& g, const CoefT<ff>& cf,
         const ff fc = cf.fc[DIR][l];
         const ff ar0 = fc * r0;
         const ff2 q = fma(mk2(fc, fc), mk2(nb.r(-l), nb.r(l)), mk2(ar0, ar0)) * (mk2(gm, gp) + un2);
-        const ff2 qs = ff2{make_float2(q.h.x, -q.h.y), make_float2(q.l.x, -q.l.y)};   // (a_l Q-, -a_l Q+)
+        const float2 sgn = make_float2(1.0f, -1.0f);   // (a_l Q-, -a_l Q+), exact
+        const ff2 qs = ff2{__fmul2_rn(q.h, sgn), __fmul2_rn(q.l, sgn)};
         Sd.add(qs);
         const ff2 am2 = mk2(lane0(qs), lane0(qs)), ap2 = mk2(lane1(qs), lane1(qs));
         Fuv.add_prod(am2, mk2(um, vm)); Fuv.add_prod(ap2, mk2(up, vp));
