@@ -72,7 +72,57 @@ __global__ void __launch_bounds__(256) k_rcp(const double* __restrict__ x, doubl
     }
 }
 
+// pair arithmetic on (a, b, c): the scalar sum, product, fused multiply-add and compensated
+// accumulation (a b + c), then the same through the packed two-lane forms with lane 0 on
+// (a, b, c) and lane 1 on (b, c, a); every result as its two floats
+__global__ void __launch_bounds__(256) k_pair(const double* __restrict__ a, const double* __restrict__ b,
+                                              const double* __restrict__ c, float* __restrict__ out, long long n) {
+    using cns::ff;
+    using cns::ff2;
+    for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x) {
+        const ff pa = cns::d_to_ff(a[t]), pb = cns::d_to_ff(b[t]), pc = cns::d_to_ff(c[t]);
+        cns::ffacc acc(pc);
+        acc.add_prod(pa, pb);
+        const ff2 x = cns::mk2(pa, pb), y = cns::mk2(pb, pc), z = cns::mk2(pc, pa);
+        cns::ffacc2 acc2(z);
+        acc2.add_prod(x, y);
+        const ff2 s2 = x + y, m2 = x * y, f2 = fma(x, y, z), d2 = acc2.value();
+        const ff r[15] = {pa, pb, pc, pa + pb, pa * pb, fma(pa, pb, pc), acc.value(),
+                          cns::lane0(s2), cns::lane0(m2), cns::lane0(f2), cns::lane0(d2),
+                          cns::lane1(s2), cns::lane1(m2), cns::lane1(f2), cns::lane1(d2)};
+        for (int q = 0; q < 15; q++) {
+            out[(t * 15 + q) * 2] = r[q].h;
+            out[(t * 15 + q) * 2 + 1] = r[q].l;
+        }
+    }
+}
+
 }  // namespace
+
+extern "C" int cns_selftest_pair(int device, const double* a, const double* b, const double* c, long long n,
+                                 float* out) {
+    if (!a || !b || !c || !out || n < 1 || n > (1LL << 24)) return CNS_ERR_INVALID;
+    if (cudaSetDevice(device) != cudaSuccess) return CNS_ERR_CUDA;
+    double* buf = nullptr;
+    float* res = nullptr;
+    const size_t nb = (size_t)n;
+    if (cudaMalloc(&buf, nb * 3 * sizeof(double)) != cudaSuccess) return CNS_ERR_OOM;
+    if (cudaMalloc(&res, nb * 30 * sizeof(float)) != cudaSuccess) {
+        cudaFree(buf);
+        return CNS_ERR_OOM;
+    }
+    cudaError_t e = cudaMemcpy(buf, a, nb * 8, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(buf + nb, b, nb * 8, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(buf + 2 * nb, c, nb * 8, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) {
+        k_pair<<<512, 256>>>(buf, buf + nb, buf + 2 * nb, res, n);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = cudaMemcpy(out, res, nb * 30 * sizeof(float), cudaMemcpyDeviceToHost);
+    cudaFree(buf);
+    cudaFree(res);
+    return e == cudaSuccess ? CNS_OK : CNS_ERR_CUDA;
+}
 
 extern "C" int cns_selftest_rcp(int device, const double* x, long long n, double* fast, double* lib) {
     if (!x || !fast || !lib || n < 1 || n > (1LL << 27)) return CNS_ERR_INVALID;

@@ -64,6 +64,7 @@ SIGNATURES = {
     "cns_dissipation": (ctypes.c_int, [_vp, _dp]),
     "cns_selftest_pow": (ctypes.c_int, [ctypes.c_int, _vp, ctypes.c_longlong, ctypes.c_double, _vp, _vp]),
     "cns_selftest_rcp": (ctypes.c_int, [ctypes.c_int, _vp, ctypes.c_longlong, _vp, _vp]),
+    "cns_selftest_pair": (ctypes.c_int, [ctypes.c_int, _vp, _vp, _vp, ctypes.c_longlong, _vp]),
     "cns_selftest_convert": (ctypes.c_int, [ctypes.c_int, _vp, _vp, ctypes.c_longlong, _vp, _vp, _vp, _vp]),
 }
 

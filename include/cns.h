@@ -375,9 +375,18 @@ CNS_API int cns_selftest_convert(int device, const double* x, const float* y, lo
 CNS_API int cns_selftest_pow(int device, const double* x, long long n, double a, double* fast, double* lib);
 
 /* Self test with no counterpart in the reference: the solver's FP64 reciprocal (an FP32
- * seed and two Newton steps, used for 1/rho in every stage update and state recovery)
- * next to the IEEE division 1.0 / x on the same n <= 2^27 host values. */
+ * seed r0 refined as r0 (1 + e + e^2), used for 1/rho in every stage update and state
+ * recovery) next to the IEEE division 1.0 / x on the same n <= 2^27 host values. */
 CNS_API int cns_selftest_rcp(int device, const double* x, long long n, double* fast, double* lib);
+
+/* Self test with no counterpart in the reference: the pair arithmetic of
+ * CNS_PREC_PAIR_RHS on n <= 2^24 host triples (a, b, c), each first split into its nearest
+ * pair. out[(t * 15 + q) * 2 + {0, 1}] holds the two floats of result q of element t:
+ * q = 0..2 the pairs of a, b, c; 3..6 a + b, a b, fma(a, b, c) and the compensated
+ * accumulation c + a b; 7..10 the same four from the packed two-lane forms, lane 0 on
+ * (a, b, c); 11..14 lane 1 on (b, c, a). */
+CNS_API int cns_selftest_pair(int device, const double* a, const double* b, const double* c, long long n,
+                              float* out);
 
 #ifdef __cplusplus
 }
