@@ -205,7 +205,7 @@ def cpu_sample(p, steps_min: int = 2, seconds: float = 12.0):
 
 
 def run_batched(args, stream_ptr, members=48, mode_req="tuned", with_other=True):
-    """BASELINE config 3: the 48-member ensemble (or its first `members`) in FP32-RHS mode,
+    """The batched ensemble of 48 Taylor-Green boxes of uneven size (or its first `members`) in FP32-RHS mode,
     in the execution mode and launch shape the autotuner picks (or the mode requested, at
     full residency); the other mode is timed beside it for the record."""
     import torch
@@ -271,7 +271,7 @@ def run_batched(args, stream_ptr, members=48, mode_req="tuned", with_other=True)
 
 
 def run_serving(args):
-    """BASELINE config 4: Poisson arrivals of advance-N-steps requests, continuous batching.
+    """The serving workload: Poisson arrivals of advance-N-steps requests, continuous batching.
     The requests' initial fields are generated once per (kind, grid) before the clock starts
     and shared by the requests of that grid (the work of a request does not depend on its
     field values: N steps of its grid)."""
@@ -361,7 +361,7 @@ def at_time(t, y, t0):
 
 
 def run_precision(args):
-    """BASELINE config 2: Taylor-Green to t_end, FP32 RHS (FP64 state, accumulation, T/p
+    """The precision study: Taylor-Green to t_end, FP32 RHS (FP64 state, accumulation, T/p
     recovery, reductions) against all-FP64; relative error of <u.u>, <rho|u|^2>/2, of the
     dissipation rate eps = -dK/dt at t_end (K = <rho|u|^2>/2) and of the viscous dissipation
     <tau_ij du_i/dx_j> at t_end (cns_dissipation)."""
