@@ -361,33 +361,37 @@ def at_time(t, y, t0):
 
 
 def run_precision(args):
-    """The precision study: Taylor-Green to t_end, FP32 RHS (FP64 state, accumulation, T/p
-    recovery, reductions) against all-FP64; relative error of <u.u>, <rho|u|^2>/2, of the
-    dissipation rate eps = -dK/dt at t_end (K = <rho|u|^2>/2) and of the viscous dissipation
-    <tau_ij du_i/dx_j> at t_end (cns_dissipation)."""
+    """The precision study: Taylor-Green to t_end, FP32 RHS (or, with --precision pair, the
+    FP32-pair RHS; FP64 state, accumulation, T/p recovery, reductions in both) against
+    all-FP64; relative error of <u.u>, <rho|u|^2>/2, of the dissipation rate eps = -dK/dt at
+    t_end (K = <rho|u|^2>/2) and of the viscous dissipation <tau_ij du_i/dx_j> at t_end
+    (cns_dissipation)."""
     from cudanavierstokes_gb300.initial import tgv_fields
-    from cudanavierstokes_gb300.params import tgv_params
+    from cudanavierstokes_gb300.params import PREC_FP32_RHS, PREC_PAIR_RHS, tgv_params
     n = int(args.grid.split(",")[0]) if args.grid else 128
+    mode, prec, dtype = (("pair_rhs", PREC_PAIR_RHS, "f32x2-rhs/f64-state vs f64") if args.precision == "pair"
+                         else ("fp32_rhs", PREC_FP32_RHS, "f32-rhs/f64-state vs f64"))
     p64 = tgv_params(n)
     f = tgv_fields(p64)
     r64 = ke_series(p64, f, args.t_end)
-    r32 = ke_series(p64.copy(precision=1), f, args.t_end)
-    res = {"eps_viscous": {"fp64": r64["eps_viscous"], "fp32_rhs": r32["eps_viscous"],
+    r32 = ke_series(p64.copy(precision=prec), f, args.t_end)
+    res = {"eps_viscous": {"fp64": r64["eps_viscous"], mode: r32["eps_viscous"],
                            "rel_err": abs(r32["eps_viscous"] - r64["eps_viscous"]) / abs(r64["eps_viscous"])}}
     for key in ("ke", "ke_rho"):
         a, da = at_time(r64["t"], r64[key], args.t_end)
         b, db = at_time(r32["t"], r32[key], args.t_end)
-        res[key] = {"fp64": a, "fp32_rhs": b, "rel_err": abs(b - a) / abs(a),
-                    "eps_fp64": -da, "eps_fp32_rhs": -db, "eps_rel_err": abs(db - da) / abs(da)}
-    line = {"metric": "kinetic-energy relative error at t_end, FP32 RHS vs FP64", "value": res["ke_rho"]["rel_err"],
-            "unit": "relative", "higher_is_better": False, "dtype": "f32-rhs/f64-state vs f64",
+        res[key] = {"fp64": a, mode: b, "rel_err": abs(b - a) / abs(a),
+                    "eps_fp64": -da, "eps_" + mode: -db, "eps_rel_err": abs(db - da) / abs(da)}
+    what = "FP32-pair RHS" if prec == PREC_PAIR_RHS else "FP32 RHS"
+    line = {"metric": f"kinetic-energy relative error at t_end, {what} vs FP64", "value": res["ke_rho"]["rel_err"],
+            "unit": "relative", "higher_is_better": False, "dtype": dtype,
             "data": "synthetic", "config": {"workload": f"Taylor-Green {n}^3, Ma 0.1, Re 1600, Pr 0.71, S=V=4, "
                                                         "Wray RK3, CFL 0.5", "t_end": args.t_end},
             "ke_uu": res["ke"], "ke_rho": res["ke_rho"], "eps_viscous": res["eps_viscous"],
             "fp64": {"steps": r64["steps"], "wall_s": r64["wall"],
                      "Mpoint_steps_per_s": p64.npoints * r64["steps"] / r64["wall"] / 1e6},
-            "fp32_rhs": {"steps": r32["steps"], "wall_s": r32["wall"],
-                         "Mpoint_steps_per_s": p64.npoints * r32["steps"] / r32["wall"] / 1e6}}
+            mode: {"steps": r32["steps"], "wall_s": r32["wall"],
+                   "Mpoint_steps_per_s": p64.npoints * r32["steps"] / r32["wall"] / 1e6}}
     print(json.dumps(line), flush=True)
 
 
