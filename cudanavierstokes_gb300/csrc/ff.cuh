@@ -191,7 +191,8 @@ inline constexpr bool is_ff = false;
 template <>
 inline constexpr bool is_ff<ff> = true;
 
-// FP64 <-> pair: h + l in FP64 is exact (48 bits); the split rounds h, then the remainder
+// FP64 <-> pair: (double)h + (double)l rounds once in FP64 (2^-53, below the pair's own
+// precision); the split rounds h, then the remainder x - h (exact in FP64)
 __device__ __forceinline__ double ff_to_d(ff x) { return (double)x.h + (double)x.l; }
 __device__ __forceinline__ ff d_to_ff(double x) {
     const float h = __double2float_rn(x);
