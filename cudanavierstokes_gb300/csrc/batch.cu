@@ -351,8 +351,8 @@ int cns_batch_create(int device, int precision, int stencil_size, int stencil_vi
                      cns_batch** out) {
     if (!out) return cns::set_error(CNS_ERR_INVALID, "out is NULL");
     *out = nullptr;
-    if (precision != CNS_PREC_FP64 && precision != CNS_PREC_FP32_RHS)
-        return cns::set_error(CNS_ERR_INVALID, "unknown precision");
+    if (precision != CNS_PREC_FP64 && precision != CNS_PREC_FP32_RHS)   // the pair mode runs single solvers only
+        return cns::set_error(CNS_ERR_INVALID, "batches run in CNS_PREC_FP64 or CNS_PREC_FP32_RHS");
     if (stencil_size < 1 || stencil_size > 4 || stencil_visc < 1 || stencil_visc > stencil_size)
         return cns::set_error(CNS_ERR_INVALID, "stencil orders out of range");
     int ndev = 0;

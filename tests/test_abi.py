@@ -50,6 +50,15 @@ def test_parameter_validation(gpu_lib):
         p = tgv_params(16).copy(**bad)
         assert gpu_lib.cns_check_params(ctypes.byref(p)) == 1, bad
         assert gpu_lib.cns_last_error().decode()
+    for prec in (0, 1, 2):   # FP64, FP32-RHS and pair mode
+        assert gpu_lib.cns_check_params(ctypes.byref(tgv_params(16).copy(precision=prec))) == 0
+
+
+def test_batch_rejects_the_pair_mode(gpu_lib):
+    """Batches take FP64 or FP32-RHS; the argument check comes before any device call."""
+    b = ctypes.c_void_p()
+    assert gpu_lib.cns_batch_create(0, 2, 4, 4, 0, ctypes.byref(b)) == 1 and not b
+    assert "CNS_PREC_FP32_RHS" in gpu_lib.cns_last_error().decode()
 
 
 def test_largest_grids(gpu_lib):
