@@ -208,12 +208,11 @@ __device__ __forceinline__ void rhs_dir_pair(const Geom& g, const CoefT<ff>& cf,
                                              ff (&acc)[5], ff (&W)[3], ff (&L)[4], ff& cond) {
     const bool nux = MAYBE_X && DIR == 0 && g.nonuniform_x;
     const ff t0 = nb.t(0);
-    if (nux) {
-        const ff cw = __ldg(cf.cvsx + V * g.mx + i);
-        L[0] = fma(cw, u0, L[0]); L[1] = fma(cw, v0, L[1]); L[2] = fma(cw, w0, L[2]); L[3] = fma(cw, t0, L[3]);
-    } else {
-        const ff cw = cf.c2V[DIR][0];
-        L[0] = fma(cw, u0, L[0]); L[1] = fma(cw, v0, L[1]); L[2] = fma(cw, w0, L[2]); L[3] = fma(cw, t0, L[3]);
+    {   // centre terms of the second derivatives
+        const ff cw = nux ? __ldg(cf.cvsx + V * g.mx + i) : cf.c2V[DIR][0];
+        const ff2 cw2 = mk2(cw, cw);
+        const ff2 luv = fma(cw2, mk2(u0, v0), mk2(L[0], L[1])), lwt = fma(cw2, mk2(w0, t0), mk2(L[2], L[3]));
+        L[0] = lane0(luv); L[1] = lane1(luv); L[2] = lane0(lwt); L[3] = lane1(lwt);
     }
     const ff un = (MAYBE_X && DIR == 0) ? u0 : (DIR == 1 ? v0 : w0);
     const ff zero(0);
@@ -261,26 +260,28 @@ __device__ __forceinline__ void rhs_dir_pair(const Geom& g, const CoefT<ff>& cf,
     const ff2 s2 = Sd.value(), fuv = Fuv.value(), fwe = Fwe.value();
     L[0] = lane0(luv); L[1] = lane1(luv); L[2] = lane0(lwt); L[3] = lane1(lwt);
     ff dmu = lane0(mt), dt = lane1(mt), dth = lane1(pth), dp = lane0(pth);
-    const ff sd = lane0(s2) + lane1(s2), fu = lane0(fuv), fv = lane1(fuv), fw = lane0(fwe), fe = lane1(fwe);
+    const ff sd = lane0(s2) + lane1(s2);
     if (nux) {
         const ff xpi = cf.xp[i];
-        dmu *= xpi; dt *= xpi; dth *= xpi; dp *= xpi;
+        const ff2 x2 = mk2(xpi, xpi), a = mt * x2, b = pth * x2;
+        dmu = lane0(a); dt = lane1(a); dp = lane0(b); dth = lane1(b);
     }
-    W[0] = fma(tau[0], dmu, W[0]);
-    W[1] = fma(tau[1], dmu, W[1]);
-    W[2] = fma(tau[2], dmu, W[2]);
-    cond = fma(dt, dmu, cond);
+    {   // W_q += tau_q dmu, cond += dT dmu (two packed multiply-adds)
+        const ff2 d2 = mk2(dmu, dmu);
+        const ff2 w01 = fma(mk2(tau[0], tau[1]), d2, mk2(W[0], W[1])), w2c = fma(mk2(tau[2], dt), d2, mk2(W[2], cond));
+        W[0] = lane0(w01); W[1] = lane1(w01); W[2] = lane0(w2c); cond = lane1(w2c);
+    }
     at3(W, MAYBE_X ? DIR : (DIR == 1 ? 1 : 2), [&](ff& w) { w = fma(m3, dth, w); });
     const ff fr = nux ? sd + sd : fma(ff(2), sd, acc[0]);
     if (nux) {
         const ff xpi = cf.xp[i];
-        acc[0] = fma(xpi, fr, acc[0]);
-        acc[1] = fma(xpi, fu, acc[1]);
-        acc[2] = fma(xpi, fv, acc[2]);
-        acc[3] = fma(xpi, fw, acc[3]);
-        acc[4] = fma(xpi, fe, acc[4]);
+        const ff2 x2 = mk2(xpi, xpi);
+        const ff2 a01 = fma(x2, mk2(fr, lane0(fuv)), mk2(acc[0], acc[1]));
+        const ff2 a23 = fma(x2, mk2(lane1(fuv), lane0(fwe)), mk2(acc[2], acc[3]));
+        acc[0] = lane0(a01); acc[1] = lane1(a01); acc[2] = lane0(a23); acc[3] = lane1(a23);
+        acc[4] = fma(xpi, lane1(fwe), acc[4]);
     } else {
-        acc[0] = fr; acc[1] = fu; acc[2] = fv; acc[3] = fw; acc[4] = fe;
+        acc[0] = fr; acc[1] = lane0(fuv); acc[2] = lane1(fuv); acc[3] = lane0(fwe); acc[4] = lane1(fwe);
     }
     if (MAYBE_X && DIR == 0) acc[1] -= dp; else if (DIR == 1) acc[2] -= dp; else acc[3] -= dp;
 }
