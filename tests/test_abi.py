@@ -54,6 +54,14 @@ def test_parameter_validation(gpu_lib):
         assert gpu_lib.cns_check_params(ctypes.byref(tgv_params(16).copy(precision=prec))) == 0
 
 
+def test_precision_constants_match_the_header():
+    from cudanavierstokes_gb300 import params
+    src = open(os.path.join(REPO, "include", "cns.h")).read()
+    defs = {m.group(1): int(m.group(2)) for m in re.finditer(r"#define CNS_(PREC_\w+)\s+(\d+)", src)}
+    assert defs == {"PREC_FP64": params.PREC_FP64, "PREC_FP32_RHS": params.PREC_FP32_RHS,
+                    "PREC_PAIR_RHS": params.PREC_PAIR_RHS}
+
+
 def test_batch_rejects_the_pair_mode(gpu_lib):
     """Batches take FP64 or FP32-RHS; the argument check comes before any device call."""
     b = ctypes.c_void_p()
