@@ -199,9 +199,10 @@ __device__ __forceinline__ void rhs_direction(const Geom& g, const CoefT<R>& cf,
 // Pair-type body of one direction: the sums of rhs_direction in one pass over the offsets
 // l = 1..S that is not unrolled (the pair arithmetic is ~15 instructions per operation, and
 // the unrolled body does not fit the instruction caches). At each l it loads the neighbours
-// on either side and feeds every sum that needs them; each sum keeps rhs_direction's order
-// (centre term, then l ascending), except the stretched-x second derivative, which adds the
-// pair (-l, l) per l.
+// on either side and feeds every sum that needs them; each sum keeps rhs_direction's terms
+// and order (centre term, then l ascending; the stretched-x second derivative adds the pair
+// (-l, l) per l) in an accumulator whose tail is normalised once at the end, two sums at a
+// time through the packed FP32x2 forms (ffacc2, ff.cuh).
 template <int S, int V, bool MAYBE_X>
 __device__ __forceinline__ void rhs_dir_pair(const Geom& g, const CoefT<ff>& cf, const NbGlobal<ff>& nb, int i,
                                              const int DIR, const ff (&tau)[3], ff m3, ff u0, ff v0, ff w0, ff r0,
