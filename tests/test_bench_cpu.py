@@ -75,3 +75,13 @@ def test_reference_arm_line(monkeypatch, capsys, oracle_mod):
     assert line["cpu_baseline"]["kind"] == "port" and line["cpu_baseline"]["cores"] >= 1
     assert line["e2e"]["h2d_bytes_per_step"] == 0 and line["e2e"]["value"] == line["value"]
     assert line["config"]["grid"] == [16, 12, 20]
+
+
+def test_precision_flag_maps_to_the_solver_modes(monkeypatch):
+    """--precision fp64 | fp32 | pair selects the solver's precision for the workload."""
+    from cudanavierstokes_gb300.params import PREC_FP32_RHS, PREC_FP64, PREC_PAIR_RHS
+    for flag, prec in (("fp64", PREC_FP64), ("fp32", PREC_FP32_RHS), ("pair", PREC_PAIR_RHS)):
+        monkeypatch.setattr(sys, "argv", ["bench.py", "--precision", flag])
+        a = bench.parse_args()
+        p, _ = bench.workload(a.workload, a.precision, a.grid)
+        assert p.precision == prec and (p.mx, p.my, p.mz) == (128, 160, 192)
